@@ -1,0 +1,409 @@
+"""Benchmark of the GB300 split-step solver.
+
+Workload (default): the real-time Raman-dressed quench on a 1024x1024
+two-component grid over [-32,32)^2 in complex64: g_uu = g_dd = 1000,
+g_ud = 990, Omega = 1, k_L = 3 (theta = 2 k_L x), prepared by 3000
+imaginary-time steps at dt = 0.01 before the timed region, then quenched to
+delta = 0.5 and propagated in real time at dt = 1e-3.  A step is one full
+Strang step (three sub-steps) of one solve; the metric is full steps per
+second.
+
+To keep the timed working set larger than the 129 MB L2, R independent
+copies of the solve (replicas, 16 MiB of state each) are stepped round-robin,
+so consecutive steps never reuse a cached state; R is chosen so that the
+replicas' states are at least twice the L2 size.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
+
+Under torchrun each rank runs its own replicas on its own GPU ("replicas
+only": a solve is never split across GPUs); the time is the maximum over
+ranks and the value counts the steps of all ranks.
+
+``--impl reference`` times the original algorithm's CPU path (the oracle's
+restatement of spinor-gpe's torch propagator) on the host cores, on the same
+workload, and also its torch CUDA path on the same GPU.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, 'spinor-gpe_gb300'))
+
+METRIC = 'full Strang steps/s @1024^2 complex64 (real-time Raman quench)'
+UNIT = 'steps/s'
+L2_BYTES = 129 * 2**20
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=1000)
+    ap.add_argument('--warmup', type=int, default=10)
+    ap.add_argument('--impl', default='native', choices=['native', 'reference'])
+    ap.add_argument('--n', type=int, default=1024, help='grid side')
+    ap.add_argument('--prep-steps', type=int, default=3000)
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ helpers
+
+def dist_setup():
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = 'nccl' if torch.cuda.is_available() else 'gloo'
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def max_over_ranks(x, world):
+    """Maximum of a float over all ranks (x itself when world == 1)."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = 'cuda' if dist.get_backend() == 'nccl' else 'cpu'
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def measured_peaks():
+    path = os.path.join(REPO, 'MEASURED_PEAKS.json')
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d['hbm_gbs']), 'measured'
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, 'fallback'
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during a region."""
+
+    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,'
+              'clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,'
+              'clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,'
+              'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix='.csv')
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.gpu), '--query-gpu=' + self.FIELDS,
+                 '--format=csv,noheader,nounits', '-lms', '100'],
+                stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unsampled']}
+        sm, smax, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown',
+                 'sw_power_cap']
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(',')]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == 'active':
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unsampled']}
+        return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': max(smax),
+                'samples': len(sm), 'reasons': sorted(reasons)}
+
+
+def build_problem(tmpdir, n, prep_steps, device, dtype=64):
+    """The 1024^2 quench workload: imaginary-time preparation at delta = 0
+    (untimed), then delta -> 0.5.  Returns the PSpinor ready for real time."""
+    import torch
+    from spinor_gpe import workloads
+    from spinor_gpe.pspinor import pspinor as spin
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    from spinor_gpe.pspinor import tensor_propagator as tprop
+    ps = workloads.raman_quench_1024(spin.PSpinor, ttools.fft_2d,
+                                     os.path.join(tmpdir, 'quench') + '/',
+                                     n=n, delta=0.0)
+    if prep_steps > 0 and device is not None:
+        prop = tprop.TensorPropagator(ps, 0.01, prep_steps, device,
+                                      time='imag', dtype=dtype)
+        prop.full_steps(prep_steps)
+        ps.psik = [p.cpu().numpy() for p in prop.psik]
+        del prop
+        torch.cuda.synchronize()
+    ps.detuning_uniform(0.5)
+    return ps
+
+
+# ------------------------------------------------------------- CPU baseline
+
+def cpu_reference_rate(ps, budget_s=12.0, max_steps=50, dtype=64):
+    """Full steps/s of the original algorithm on the host cores (the oracle's
+    torch restatement, all intra-op threads), on a bounded sample."""
+    import torch
+    sys.path.insert(0, REPO)
+    from oracle import OraclePropagator, OracleInputs
+    torch.set_num_threads(os.cpu_count() or 1)
+    inp = OracleInputs(
+        psik=[np.asarray(p) for p in ps.psik],
+        kin_eng_spin=[np.asarray(k) for k in ps.kin_eng_spin],
+        pot_eng_spin=[np.asarray(v) for v in ps.pot_eng_spin],
+        coupling=np.asarray(ps.coupling, dtype=np.float64),
+        x_mesh=ps.space['x_mesh'], dr=ps.space['dr'],
+        dv_r=float(ps.space['dv_r']), dv_k=float(ps.space['dv_k']),
+        g_sc=dict(ps.g_sc), atom_num=float(ps.atom_num),
+        kL_recoil=float(ps.kL_recoil), rot_coupling=bool(ps.rot_coupling),
+        is_coupling=bool(ps.is_coupling))
+    orc = OraclePropagator(inp, 1e-3, 'real', dtype)
+    orc.full_step()                       # warm-up
+    t0 = time.perf_counter()
+    orc.full_step()
+    one = time.perf_counter() - t0
+    n = int(max(2, min(max_steps, budget_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    for _ in range(n):
+        orc.full_step()
+    dt = time.perf_counter() - t0
+    return {'value': n / dt, 'unit': UNIT, 'cores': torch.get_num_threads(),
+            'kind': 'port',
+            'sample': f'{n} real-time full steps of one {ps.psik[0].shape[0]}^2 '
+                      f'complex64 solve (the oracle, torch CPU, '
+                      f'{torch.get_num_threads()} threads)'}, inp
+
+
+def torch_cuda_reference_rate(inp, steps=30, warmup=3, dtype=64):
+    """Full steps/s of the original algorithm's torch CUDA path (the oracle's
+    restatement run on the GPU: torch.fft, ATen element-wise kernels and the
+    original's host synchronisations)."""
+    import torch
+    from oracle import OraclePropagator
+    orc = OraclePropagator(inp, 1e-3, 'real', dtype, device='cuda')
+    for _ in range(warmup):
+        orc.full_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        orc.full_step()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return steps / dt
+
+
+# --------------------------------------------------------------- native arm
+
+def run_native(args, world, rank, local):
+    import torch
+    from spinor_gpe.pspinor import tensor_propagator as tprop
+    torch.cuda.set_device(local)
+    device = f'cuda:{local}'
+    n = args.n
+    tmp = tempfile.mkdtemp(prefix='sgpe_bench_')
+    ps = build_problem(tmp, n, args.prep_steps, device)
+    state_bytes = 2 * n * n * 8
+    n_rep = max(1, math.ceil(2 * L2_BYTES / state_bytes) + 1)
+    psik_host = [torch.as_tensor(np.asarray(p), dtype=torch.complex64)
+                 .pin_memory() for p in ps.psik]
+    props = [tprop.TensorPropagator(ps, 1e-3, args.steps, device, time='real',
+                                    dtype=64) for _ in range(n_rep)]
+    stream = torch.cuda.current_stream()
+
+    # warm-up
+    for i in range(args.warmup):
+        props[i % n_rep].full_steps(1)
+    torch.cuda.synchronize()
+
+    # ---- device-timed region: K steps round-robin over the replicas
+    k = args.steps
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for i in range(k):
+            props[i % n_rep].full_steps(1)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    t_dev = ev0.elapsed_time(ev1) / 1e3
+    t_max = max_over_ranks(t_dev, world)
+    value = world * k / t_max
+
+    # ---- per-pass roofline (same workload, events around every pass)
+    col_ms, row_ms = props[0]._plan.time_passes(torch, 50, props[0]._device)
+
+    # ---- end to end through the public API, host buffers
+    pops_dev = [torch.empty((k, 2), dtype=torch.float64, device=device)
+                for _ in range(n_rep)]
+    pops_host = torch.empty((k, 2), dtype=torch.float64).pin_memory()
+    out_host = [[torch.empty((n, n), dtype=torch.complex64).pin_memory()
+                 for _ in range(2)] for _ in range(n_rep)]
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for r in range(n_rep):
+        props[r].psik = [h.to(device, non_blocking=True) for h in psik_host]
+    for i in range(k):
+        r = i % n_rep
+        j = i // n_rep
+        props[r].full_steps(1, pops_dev[r][j:j + 1])
+        if j > 0:   # populations of the replica's previous step are final now
+            pops_host[i - n_rep].copy_(pops_dev[r][j - 1], non_blocking=True)
+    for r in range(n_rep):
+        for c in range(2):
+            out_host[r][c].copy_(props[r].psik[c], non_blocking=True)
+    torch.cuda.synchronize()
+    t_e2e = max_over_ranks(time.perf_counter() - t0, world)
+    h2d = n_rep * state_bytes / k
+    d2h = (n_rep * state_bytes + 16 * (k - n_rep)) / k
+    assert np.isfinite(out_host[0][0].numpy()).all()
+
+    peak, peak_kind = measured_peaks()
+    pass_bytes = 4 * n * n * 8            # read + write of both components
+    dom_ms, dom_name = max((row_ms, 'row_kernel'), (col_ms, 'col_kernel'))
+    achieved = pass_bytes / (dom_ms / 1e3) / 1e9
+    step_bytes = 48 * n * n * 8           # 12 sweeps per full step (reference count)
+    traffic = None
+    tpath = os.path.join(REPO, 'profiles', 'traffic.json')
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get(dom_name)
+        except ValueError:
+            traffic = None
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu, _ = cpu_reference_rate(ps)
+
+    line = {
+        'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world,
+        'steps': k, 'warmup': args.warmup,
+        'ms_per_step': 1e3 * t_max / k * 1.0,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'c64 (fp32 butterflies; fp64 reductions)',
+        'data': 'synthetic (seeded Thomas-Fermi + phase noise, 3000-step '
+                'imaginary-time preparation)',
+        'config': {'workload': f'raman_quench_{n}', 'grid': [n, n],
+                   'time': 'real', 'dt': 1e-3, 'delta': 0.5, 'omega': 1.0,
+                   'k_L': 3.0, 'g': [1000.0, 1000.0, 990.0],
+                   'replicas_per_gpu': n_rep,
+                   'l2': f'inputs larger than L2: {n_rep} replica states of '
+                         f'{state_bytes >> 20} MiB stepped round-robin',
+                   'parallelism': f'replicas x{world}'},
+        'grid_point_steps_per_s': value * n * n,
+        'e2e': {'value': world * k / t_e2e, 'unit': UNIT,
+                'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h,
+                'path': 'TensorPropagator.psik= (H2D, pinned) / full_steps(1) '
+                        'per step with per-step populations D2H / psik D2H'},
+        'roofline': {'bound': 'hbm', 'kernel': dom_name,
+                     'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                     'frac': achieved / peak, 'traffic': traffic,
+                     'peak_kind': peak_kind,
+                     'algorithmic_bytes': pass_bytes,
+                     'col_pass_ms': col_ms, 'row_pass_ms': row_ms},
+        'step_roofline': {'bytes_per_step': step_bytes,
+                          'achieved': value / world * step_bytes / 1e9,
+                          'peak': peak, 'unit': 'GB/s',
+                          'frac': value / world * step_bytes / 1e9 / peak},
+        'gpu_launches': 6 * k,
+        'clocks': clk.summary(),
+    }
+    if cpu is not None:
+        line['cpu_baseline'] = cpu
+    if rank == 0:
+        print(json.dumps(line))
+
+
+# ------------------------------------------------------------ reference arm
+
+def run_reference(args, world, rank, local):
+    """The original algorithm on the host cores (rank 0 only)."""
+    if rank != 0:
+        return
+    import torch
+    tmp = tempfile.mkdtemp(prefix='sgpe_ref_')
+    has_gpu = torch.cuda.is_available()
+    # no preparation here: this arm runs none of the native kernels, and the
+    # step cost does not depend on the state's values
+    ps = build_problem(tmp, args.n, 0, None)
+    cpu, inp = cpu_reference_rate(ps, budget_s=min(60.0, 3.0 * max(args.steps, 1)),
+                                  max_steps=max(args.steps, 2))
+    line = {
+        'impl': 'reference', 'metric': METRIC, 'value': cpu['value'],
+        'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': 1e3 / cpu['value'],
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'c64', 'data': 'synthetic',
+        'config': {'workload': f'raman_quench_{args.n}',
+                   'grid': [args.n, args.n], 'time': 'real', 'dt': 1e-3},
+        'cpu_baseline': cpu,
+        'e2e': {'value': cpu['value'], 'unit': UNIT, 'h2d_bytes_per_step': 0,
+                'd2h_bytes_per_step': 0},
+    }
+    if has_gpu:
+        line['torch_cuda_same_gpu'] = {
+            'value': torch_cuda_reference_rate(inp), 'unit': UNIT,
+            'what': 'original algorithm on torch CUDA (torch.fft + ATen, with '
+                    'its per-sub-step host synchronisations), complex64'}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == 'reference':
+        run_reference(args, world, rank, local)
+    else:
+        run_native(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

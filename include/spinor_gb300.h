@@ -1,0 +1,142 @@
+/*
+ * spinor_gb300.h -- C ABI of the GB300 split-step solver for the
+ * pseudospin-1/2 Gross-Pitaevskii equation.
+ *
+ * The library replaces the torch propagation path of spinor-gpe
+ * (spinor_gpe/pspinor/tensor_propagator.py, spinor_gpe/pspinor/tensor_tools.py).
+ * It exposes plain C: opaque plan handles, plain pointers and sizes, an int
+ * status on every call (0 = success) and a thread-local message from
+ * sgpe_last_error().  No exception crosses this boundary.
+ *
+ * Conventions
+ *  - A spinor is two components, each an (ny, nx) row-major array with x
+ *    contiguous (spinor_gpe/pspinor/pspinor.py:194, 350-351).
+ *  - psik arguments are in the centred (fftshift) k order of the original
+ *    (spinor_gpe/pspinor/tensor_tools.py:218-226).
+ *  - Element type is interleaved complex: float pairs for dtype_bits = 64
+ *    (complex64), double pairs for dtype_bits = 128 (complex128).
+ *  - Device pointers live on the plan's device; "stream" is a cudaStream_t
+ *    passed as void* (NULL = legacy default stream).  All work is enqueued
+ *    asynchronously on that stream; nothing synchronises the host except the
+ *    set-up calls marked "synchronous".
+ *  - A plan is used by one host thread at a time.
+ */
+#ifndef SPINOR_GB300_H
+#define SPINOR_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SGPE_OK 0
+#define SGPE_ERR_ARG 1     /* invalid argument or unsupported size */
+#define SGPE_ERR_STATE 2   /* call not valid in the plan's current state */
+#define SGPE_ERR_CUDA 3    /* CUDA runtime error (message has the detail) */
+#define SGPE_ERR_OOM 4     /* device allocation failed */
+
+typedef struct sgpe_plan sgpe_plan;
+
+/* A complex operator field in FP64 on the host, interleaved (re, im).
+ * value(x, y) = data[x*sx + y*sy]; sx = sy = 0 is a uniform value, (1, 0) a
+ * table along x, (0, 1) a table along y, (1, nx) a full (ny, nx) field.
+ * n is the number of complex elements in data.  The library rounds the
+ * values once to the plan's precision. */
+typedef struct sgpe_field {
+  const double* data;
+  int n;
+  int sx;
+  int sy;
+} sgpe_field;
+
+/* Operators of one Strang sub-step (outer = 0, inner = 1).
+ * Replaces the pre-computed operator dicts eng_out / eng_in of the original
+ * (spinor_gpe/pspinor/tensor_propagator.py:138-149; operators built by
+ * tensor_tools.evolution_op :546-560 and coupling_op :563-591).
+ *  kin_a[c] * kin_b[c] = exp(-i K_c t/2) in NATURAL (unshifted) k order,
+ *  pot_a[c] * pot_b[c] = exp(-i V_c t) in real space,
+ *  cpl_c = cos(Omega t/4), cpl_s = -i sin(Omega t/4), cpl_e = exp(i theta),
+ *  interaction operator exp(z E_c) with z = int_z_re + i int_z_im = -i t/2.
+ * t is the (complex, in imaginary time) sub-step duration. */
+typedef struct sgpe_substep_ops {
+  sgpe_field kin_a[2];
+  sgpe_field kin_b[2];
+  sgpe_field pot_a[2];
+  sgpe_field pot_b[2];
+  sgpe_field cpl_c;
+  sgpe_field cpl_s;
+  sgpe_field cpl_e;
+  double int_z_re;
+  double int_z_im;
+} sgpe_substep_ops;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int sgpe_version(void);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* sgpe_last_error(void);
+
+/* Create a plan for an (ny, nx) grid.  Sizes: powers of two, 32..4096 on
+ * each axis.  dtype_bits: 64 (complex64) or 128 (complex128).  Allocates the
+ * device state on `device`.  Synchronous.
+ * Replaces: TensorPropagator.__init__ tensor uploads
+ * (spinor_gpe/pspinor/tensor_propagator.py:111-122). */
+int sgpe_plan_create(sgpe_plan** plan, int ny, int nx, int dtype_bits, int device);
+
+/* Release a plan and its device memory.  Synchronous. */
+int sgpe_plan_destroy(sgpe_plan* plan);
+
+/* Interaction strengths, atom number, volume elements and the coupling
+ * switch (spinor_gpe/pspinor/tensor_propagator.py:110-113, 119-121). */
+int sgpe_set_physics(sgpe_plan* plan, double g_uu, double g_dd, double g_ud,
+                     double atom_num, double dv_r, double dv_k, int is_coupling);
+
+/* Upload the operators of sub-step `sub` (0 = outer, 1 = inner).
+ * Synchronous.  Replaces: tensor_propagator.py:138-149. */
+int sgpe_set_substep(sgpe_plan* plan, int sub, const sgpe_substep_ops* ops);
+
+/* Load a spinor (device pointers, centred k order) as the plan state.
+ * Replaces: assignment of TensorPropagator.psik (tensor_propagator.py:118). */
+int sgpe_load_psik(sgpe_plan* plan, const void* psik0, const void* psik1, void* stream);
+
+/* Write the current state as psik (device pointers, centred k order),
+ * renormalised to the atom number in k-space as the original leaves it after
+ * every sub-step (tensor_propagator.py:271).  If pops_dev is non-NULL, the two
+ * component populations (tensor_tools.calc_pops, :466-484) of that state are
+ * written there as doubles.  The plan state is not changed. */
+int sgpe_store_psik(sgpe_plan* plan, void* psik0, void* psik1, double* pops_dev, void* stream);
+
+/* One Strang sub-step with the operators of `sub`.
+ * Replaces: TensorPropagator.single_step (tensor_propagator.py:224-271). */
+int sgpe_single_step(sgpe_plan* plan, int sub, void* stream);
+
+/* n_steps full steps (outer, inner, outer sub-steps each).  If pops_dev is
+ * non-NULL it receives the populations after step i as pops_dev[2*i + c].
+ * Those of steps 0 .. n_steps-2 are written during the call; those of the
+ * last step are written by the next call that evaluates the state (the next
+ * sgpe_store_psik with pops_dev = NULL, or the first sub-step of the next
+ * sgpe_single_step / sgpe_full_steps), so pops_dev must stay valid until
+ * then.  sgpe_load_psik discards that pending write.
+ * Replaces: TensorPropagator.full_step (tensor_propagator.py:214-222) and the
+ * step loop of prop_loop (:185-194). */
+int sgpe_full_steps(sgpe_plan* plan, int n_steps, double* pops_dev, void* stream);
+
+/* Normalised, centred 2-D transforms of a two-component field (device
+ * pointers, out-of-place; in and out must not overlap).
+ *   inverse = 0: out_c = scale * fftshift(fft2(in_c))       (fft_2d, tensor_tools.py:201-228)
+ *   inverse = 1: out_c = scale * ifft2_unnormalised(ifftshift(in_c))
+ *                (ifft_2d, tensor_tools.py:231-258, with scale = 1/(nx ny norm))
+ * Does not touch the propagation state. */
+int sgpe_fft2(sgpe_plan* plan, const void* in0, const void* in1, void* out0, void* out1,
+              int inverse, double scale, void* stream);
+
+/* Measurement helper: n_steps full steps exactly as sgpe_full_steps (no
+ * populations), with CUDA events recorded on `stream` around every column
+ * pass and every row pass.  Synchronises the stream and returns the mean
+ * duration of one column pass and of one row pass in milliseconds.
+ * Instrumentation of the native path; no counterpart in the original. */
+int sgpe_time_passes(sgpe_plan* plan, int n_steps, double* col_ms, double* row_ms, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPINOR_GB300_H */

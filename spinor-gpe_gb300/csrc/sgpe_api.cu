@@ -1,0 +1,555 @@
+// C ABI of the split-step solver: plan life cycle, operator upload and the
+// sequencing of column/row passes that makes up the Strang steps of
+// spinor_gpe/pspinor/tensor_propagator.py:214-271.
+//
+// State machine of a plan:
+//   EMPTY --load_psik--> KSPACE (natural-order psik in the state buffers)
+//   KSPACE/MIXED --single_step--> MIXED (x-forward-transformed state after a
+//                                        row pass; see sgpe_kernels.cuh)
+// store_psik materialises psik from MIXED (column pass + renormalisation)
+// without changing the state.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sgpe_launch.cuh"
+#include "spinor_gb300.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  return fail(SGPE_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+struct DevField {
+  void* p = nullptr;
+  int sx = 0, sy = 0;
+};
+
+struct SubOps {
+  DevField kin_a[2], kin_b[2], pot_a[2], pot_b[2], cc, cs, ce;
+  double zr = 0.0, zi = 0.0;
+  std::vector<void*> allocs;
+  bool set = false;
+};
+
+enum Form { kEmpty = 0, kKspace = 1, kMixed = 2 };
+
+// Restores the caller's current device on scope exit.
+struct DeviceGuard {
+  int prev = -1;
+  bool ok = false;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) == cudaSuccess && cudaSetDevice(dev) == cudaSuccess) ok = true;
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+}  // namespace
+
+struct sgpe_plan {
+  int ny = 0, nx = 0, bits = 0, device = 0;
+  size_t elem = 0;           // bytes per complex element
+  void* s[2] = {nullptr, nullptr};
+  void* scratch[2] = {nullptr, nullptr};
+  double* part = nullptr;    // column-pass partial sums [2][ntile][2]
+  int ntile = 0;
+  void* tw_x = nullptr;
+  void* tw_y = nullptr;
+  SubOps sub[2];
+  double g[3] = {0, 0, 0};
+  double atom_num = 1.0, dv_r = 1.0, dv_k = 1.0;
+  int coupling = 0;
+  bool physics = false;
+  int form = kEmpty;
+  int prev_sub = 0;
+  // Device slot that receives the populations of the current (mixed) state
+  // when they are next computed: set by sgpe_full_steps for its last step.
+  double* pending_pops = nullptr;
+};
+
+namespace {
+
+template <typename R> void* upload_twiddles(int n, cudaError_t* err) {
+  using C = sgpe::Cx<R>;
+  std::vector<C> h(n);
+  const double two_pi = 6.283185307179586476925286766559;
+  for (int i = 0; i < n; ++i) {
+    const double ang = two_pi * double(i) / double(n);
+    h[i].x = R(std::cos(ang));
+    h[i].y = R(-std::sin(ang));
+  }
+  void* d = nullptr;
+  *err = cudaMalloc(&d, sizeof(C) * n);
+  if (*err != cudaSuccess) return nullptr;
+  *err = cudaMemcpy(d, h.data(), sizeof(C) * n, cudaMemcpyHostToDevice);
+  return d;
+}
+
+void free_sub(SubOps& so) {
+  for (void* p : so.allocs) cudaFree(p);
+  so = SubOps();
+}
+
+int upload_field(sgpe_plan* p, const sgpe_field& f, DevField* out, SubOps* so, const char* name) {
+  if (f.data == nullptr || f.n < 1 || f.sx < 0 || f.sy < 0)
+    return fail(SGPE_ERR_ARG, std::string("field ") + name + ": null data, empty or negative stride");
+  const long long last = (long long)(p->nx - 1) * f.sx + (long long)(p->ny - 1) * f.sy;
+  if (last >= f.n) return fail(SGPE_ERR_ARG, std::string("field ") + name + ": strides exceed its data");
+  void* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, p->elem * f.n);
+  if (e != cudaSuccess) return fail(SGPE_ERR_OOM, std::string("field ") + name + ": " + cudaGetErrorString(e));
+  so->allocs.push_back(d);
+  if (p->bits == 64) {
+    std::vector<float> h(2 * (size_t)f.n);
+    for (size_t i = 0; i < h.size(); ++i) h[i] = float(f.data[i]);
+    e = cudaMemcpy(d, h.data(), p->elem * f.n, cudaMemcpyHostToDevice);
+  } else {
+    e = cudaMemcpy(d, f.data, p->elem * f.n, cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "field upload");
+  out->p = d;
+  out->sx = f.sx;
+  out->sy = f.sy;
+  return SGPE_OK;
+}
+
+template <typename R> sgpe::Field<R> typed(const DevField& f) {
+  return sgpe::Field<R>{static_cast<const sgpe::Cx<R>*>(f.p), f.sx, f.sy};
+}
+
+template <typename R> sgpe::KinOp<R> kin_op(const SubOps& so) {
+  sgpe::KinOp<R> k;
+  for (int c = 0; c < 2; ++c) {
+    k.a[c] = typed<R>(so.kin_a[c]);
+    k.b[c] = typed<R>(so.kin_b[c]);
+  }
+  return k;
+}
+
+template <typename R> sgpe::RealOp<R> real_op(const SubOps& so) {
+  sgpe::RealOp<R> o;
+  for (int c = 0; c < 2; ++c) {
+    o.pa[c] = typed<R>(so.pot_a[c]);
+    o.pb[c] = typed<R>(so.pot_b[c]);
+  }
+  o.cc = typed<R>(so.cc);
+  o.cs = typed<R>(so.cs);
+  o.ce = typed<R>(so.ce);
+  o.zr = R(so.zr);
+  o.zi = R(so.zi);
+  return o;
+}
+
+template <typename R> sgpe::Cx<R>* st(void* p) { return static_cast<sgpe::Cx<R>*>(p); }
+template <typename R> const sgpe::Cx<R>* cst(const void* p) { return static_cast<const sgpe::Cx<R>*>(p); }
+
+// Column pass over the state (in place) ending a sub-step and starting `sub`.
+template <typename R> cudaError_t col_pass_step(sgpe_plan* p, int sub, cudaStream_t s) {
+  sgpe::ColArgs<R> a{};
+  a.in[0] = cst<R>(p->s[0]);
+  a.in[1] = cst<R>(p->s[1]);
+  a.out[0] = st<R>(p->s[0]);
+  a.out[1] = st<R>(p->s[1]);
+  a.tw = cst<R>(p->tw_y);
+  a.nx = p->nx;
+  a.fwd = (p->form == kMixed);
+  a.inv = 1;
+  a.has_kprev = (p->form == kMixed);
+  if (a.has_kprev) a.kprev = kin_op<R>(p->sub[p->prev_sub]);
+  a.has_knext = 1;
+  a.knext = kin_op<R>(p->sub[sub]);
+  a.scale = R(1);
+  a.part = p->part;
+  return sgpe::launch_col<R>(a, p->ny, s);
+}
+
+template <typename R> cudaError_t row_pass_step(sgpe_plan* p, int sub, double* pops, cudaStream_t s) {
+  sgpe::RowArgs<R> a{};
+  a.in[0] = cst<R>(p->s[0]);
+  a.in[1] = cst<R>(p->s[1]);
+  a.out[0] = st<R>(p->s[0]);
+  a.out[1] = st<R>(p->s[1]);
+  a.tw = cst<R>(p->tw_x);
+  a.mode = sgpe::kRowStep;
+  a.scale = R(1);
+  a.part = p->part;
+  a.ntile = p->ntile;
+  a.norm_num = p->atom_num / (double(p->nx) * double(p->ny) * p->dv_r);
+  a.g_uu = R(p->g[0]);
+  a.g_dd = R(p->g[1]);
+  a.g_ud = R(p->g[2]);
+  a.coupling = p->coupling;
+  a.op = real_op<R>(p->sub[sub]);
+  a.pops = pops;
+  a.atom_num = p->atom_num;
+  return sgpe::launch_row<R>(a, p->nx, p->ny, s);
+}
+
+template <typename R> int substep(sgpe_plan* p, int sub, double* pops, cudaStream_t s) {
+  const bool fused = (p->form == kMixed);
+  if (fused && pops == nullptr) pops = p->pending_pops;
+  p->pending_pops = nullptr;
+  cudaError_t e = col_pass_step<R>(p, sub, s);
+  if (e != cudaSuccess) return cuda_fail(e, "column pass");
+  e = row_pass_step<R>(p, sub, fused ? pops : nullptr, s);
+  if (e != cudaSuccess) return cuda_fail(e, "row pass");
+  p->form = kMixed;
+  p->prev_sub = sub;
+  return SGPE_OK;
+}
+
+template <typename R> int store(sgpe_plan* p, void* o0, void* o1, double* pops, cudaStream_t s) {
+  if (p->form == kKspace) {
+    sgpe::CopyArgs<R> c{};
+    c.in[0] = cst<R>(p->s[0]);
+    c.in[1] = cst<R>(p->s[1]);
+    c.out[0] = st<R>(o0);
+    c.out[1] = st<R>(o1);
+    c.nx = p->nx;
+    c.ny = p->ny;
+    c.shift = 1;
+    c.scale = R(1);
+    cudaError_t e = sgpe::launch_copy<R>(c, s);
+    return e == cudaSuccess ? SGPE_OK : cuda_fail(e, "store (copy)");
+  }
+  sgpe::ColArgs<R> a{};
+  a.in[0] = cst<R>(p->s[0]);
+  a.in[1] = cst<R>(p->s[1]);
+  a.out[0] = st<R>(o0);
+  a.out[1] = st<R>(o1);
+  a.tw = cst<R>(p->tw_y);
+  a.nx = p->nx;
+  a.fwd = 1;
+  a.inv = 0;
+  a.out_shift = 1;
+  a.has_kprev = 1;
+  a.kprev = kin_op<R>(p->sub[p->prev_sub]);
+  a.has_knext = 0;
+  a.scale = R(1);
+  a.part = p->part;
+  cudaError_t e = sgpe::launch_col<R>(a, p->ny, s);
+  if (e != cudaSuccess) return cuda_fail(e, "store (column pass)");
+  sgpe::ScaleArgs<R> sa{};
+  sa.d[0] = st<R>(o0);
+  sa.d[1] = st<R>(o1);
+  sa.n = (long long)p->nx * p->ny;
+  sa.part = p->part;
+  sa.ntile = p->ntile;
+  sa.atom_num = p->atom_num;
+  sa.dv = p->dv_k;
+  sa.pops = pops != nullptr ? pops : p->pending_pops;
+  p->pending_pops = nullptr;
+  e = sgpe::launch_scale<R>(sa, s);
+  return e == cudaSuccess ? SGPE_OK : cuda_fail(e, "store (scale)");
+}
+
+template <typename R> int fft2(sgpe_plan* p, const void* i0, const void* i1, void* o0, void* o1,
+                               int inverse, double scale, cudaStream_t s) {
+  if (p->scratch[0] == nullptr) {
+    for (int c = 0; c < 2; ++c) {
+      cudaError_t e = cudaMalloc(&p->scratch[c], p->elem * p->nx * p->ny);
+      if (e != cudaSuccess) return fail(SGPE_ERR_OOM, std::string("fft2 scratch: ") + cudaGetErrorString(e));
+    }
+  }
+  sgpe::RowArgs<R> r{};
+  r.tw = cst<R>(p->tw_x);
+  sgpe::ColArgs<R> c{};
+  c.tw = cst<R>(p->tw_y);
+  c.nx = p->nx;
+  c.scale = R(1);
+  c.part = nullptr;
+  cudaError_t e;
+  if (!inverse) {
+    r.in[0] = cst<R>(i0);
+    r.in[1] = cst<R>(i1);
+    r.out[0] = st<R>(p->scratch[0]);
+    r.out[1] = st<R>(p->scratch[1]);
+    r.mode = sgpe::kRowForward;
+    r.scale = R(1);
+    e = sgpe::launch_row<R>(r, p->nx, p->ny, s);
+    if (e != cudaSuccess) return cuda_fail(e, "fft2 row pass");
+    c.in[0] = cst<R>(p->scratch[0]);
+    c.in[1] = cst<R>(p->scratch[1]);
+    c.out[0] = st<R>(o0);
+    c.out[1] = st<R>(o1);
+    c.fwd = 1;
+    c.out_shift = 1;
+    c.scale = R(scale);
+    e = sgpe::launch_col<R>(c, p->ny, s);
+    if (e != cudaSuccess) return cuda_fail(e, "fft2 column pass");
+  } else {
+    c.in[0] = cst<R>(i0);
+    c.in[1] = cst<R>(i1);
+    c.out[0] = st<R>(p->scratch[0]);
+    c.out[1] = st<R>(p->scratch[1]);
+    c.inv = 1;
+    c.in_shift = 1;
+    e = sgpe::launch_col<R>(c, p->ny, s);
+    if (e != cudaSuccess) return cuda_fail(e, "ifft2 column pass");
+    r.in[0] = cst<R>(p->scratch[0]);
+    r.in[1] = cst<R>(p->scratch[1]);
+    r.out[0] = st<R>(o0);
+    r.out[1] = st<R>(o1);
+    r.mode = sgpe::kRowInverse;
+    r.scale = R(scale);
+    e = sgpe::launch_row<R>(r, p->nx, p->ny, s);
+    if (e != cudaSuccess) return cuda_fail(e, "ifft2 row pass");
+  }
+  return SGPE_OK;
+}
+
+bool ready(sgpe_plan* p) { return p->physics && p->sub[0].set && p->sub[1].set; }
+
+}  // namespace
+
+extern "C" {
+
+int sgpe_version(void) { return 100; }
+
+const char* sgpe_last_error(void) { return g_last_error.c_str(); }
+
+int sgpe_plan_create(sgpe_plan** out, int ny, int nx, int dtype_bits, int device) {
+  if (out == nullptr) return fail(SGPE_ERR_ARG, "plan output pointer is null");
+  *out = nullptr;
+  if (!sgpe::size_supported(nx) || !sgpe::size_supported(ny))
+    return fail(SGPE_ERR_ARG, "grid sizes must be powers of two in [32, 4096], got ny=" + std::to_string(ny) +
+                                  " nx=" + std::to_string(nx));
+  if (dtype_bits != 64 && dtype_bits != 128) return fail(SGPE_ERR_ARG, "dtype_bits must be 64 or 128");
+  DeviceGuard g(device);
+  if (!g.ok) return fail(SGPE_ERR_ARG, "cannot select device " + std::to_string(device));
+  sgpe_plan* p = new sgpe_plan();
+  p->ny = ny;
+  p->nx = nx;
+  p->bits = dtype_bits;
+  p->device = device;
+  p->elem = dtype_bits == 64 ? sizeof(float2) : sizeof(double2);
+  const int cols = dtype_bits == 64 ? sgpe::col_tile_width<float>(ny) : sgpe::col_tile_width<double>(ny);
+  if (cols == 0 || nx % cols != 0 || (nx / 2) % cols != 0) {
+    delete p;
+    return fail(SGPE_ERR_ARG, "nx incompatible with the column tile width");
+  }
+  p->ntile = nx / cols;
+  cudaError_t e = cudaSuccess;
+  for (int c = 0; c < 2 && e == cudaSuccess; ++c) e = cudaMalloc(&p->s[c], p->elem * (size_t)nx * ny);
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&p->part), sizeof(double) * 4 * p->ntile);
+  if (e == cudaSuccess) e = cudaMemset(p->part, 0, sizeof(double) * 4 * p->ntile);
+  if (e == cudaSuccess) {
+    if (dtype_bits == 64) {
+      p->tw_x = upload_twiddles<float>(nx, &e);
+      if (e == cudaSuccess) p->tw_y = upload_twiddles<float>(ny, &e);
+    } else {
+      p->tw_x = upload_twiddles<double>(nx, &e);
+      if (e == cudaSuccess) p->tw_y = upload_twiddles<double>(ny, &e);
+    }
+  }
+  if (e != cudaSuccess) {
+    sgpe_plan_destroy(p);
+    return fail(SGPE_ERR_OOM, std::string("plan allocation: ") + cudaGetErrorString(e));
+  }
+  *out = p;
+  return SGPE_OK;
+}
+
+int sgpe_plan_destroy(sgpe_plan* p) {
+  if (p == nullptr) return SGPE_OK;
+  DeviceGuard g(p->device);
+  for (int c = 0; c < 2; ++c) {
+    if (p->s[c]) cudaFree(p->s[c]);
+    if (p->scratch[c]) cudaFree(p->scratch[c]);
+  }
+  if (p->part) cudaFree(p->part);
+  if (p->tw_x) cudaFree(p->tw_x);
+  if (p->tw_y) cudaFree(p->tw_y);
+  free_sub(p->sub[0]);
+  free_sub(p->sub[1]);
+  delete p;
+  return SGPE_OK;
+}
+
+int sgpe_set_physics(sgpe_plan* p, double g_uu, double g_dd, double g_ud, double atom_num, double dv_r,
+                     double dv_k, int is_coupling) {
+  if (p == nullptr) return fail(SGPE_ERR_ARG, "null plan");
+  if (!(atom_num > 0) || !(dv_r > 0) || !(dv_k > 0))
+    return fail(SGPE_ERR_ARG, "atom_num, dv_r and dv_k must be positive");
+  p->g[0] = g_uu;
+  p->g[1] = g_dd;
+  p->g[2] = g_ud;
+  p->atom_num = atom_num;
+  p->dv_r = dv_r;
+  p->dv_k = dv_k;
+  p->coupling = is_coupling ? 1 : 0;
+  p->physics = true;
+  return SGPE_OK;
+}
+
+int sgpe_set_substep(sgpe_plan* p, int sub, const sgpe_substep_ops* ops) {
+  if (p == nullptr || ops == nullptr) return fail(SGPE_ERR_ARG, "null plan or operators");
+  if (sub != 0 && sub != 1) return fail(SGPE_ERR_ARG, "sub must be 0 (outer) or 1 (inner)");
+  DeviceGuard g(p->device);
+  SubOps so;
+  int rc = SGPE_OK;
+  const char* names[2] = {"0", "1"};
+  for (int c = 0; c < 2 && rc == SGPE_OK; ++c) {
+    rc = upload_field(p, ops->kin_a[c], &so.kin_a[c], &so, (std::string("kin_a") + names[c]).c_str());
+    if (rc == SGPE_OK) rc = upload_field(p, ops->kin_b[c], &so.kin_b[c], &so, "kin_b");
+    if (rc == SGPE_OK) rc = upload_field(p, ops->pot_a[c], &so.pot_a[c], &so, "pot_a");
+    if (rc == SGPE_OK) rc = upload_field(p, ops->pot_b[c], &so.pot_b[c], &so, "pot_b");
+  }
+  if (rc == SGPE_OK) rc = upload_field(p, ops->cpl_c, &so.cc, &so, "cpl_c");
+  if (rc == SGPE_OK) rc = upload_field(p, ops->cpl_s, &so.cs, &so, "cpl_s");
+  if (rc == SGPE_OK) rc = upload_field(p, ops->cpl_e, &so.ce, &so, "cpl_e");
+  if (rc != SGPE_OK) {
+    free_sub(so);
+    return rc;
+  }
+  so.zr = ops->int_z_re;
+  so.zi = ops->int_z_im;
+  so.set = true;
+  free_sub(p->sub[sub]);
+  p->sub[sub] = std::move(so);
+  return SGPE_OK;
+}
+
+int sgpe_load_psik(sgpe_plan* p, const void* k0, const void* k1, void* stream) {
+  if (p == nullptr || k0 == nullptr || k1 == nullptr) return fail(SGPE_ERR_ARG, "null plan or psik pointer");
+  DeviceGuard g(p->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (p->bits == 64) {
+    sgpe::CopyArgs<float> c{};
+    c.in[0] = cst<float>(k0);
+    c.in[1] = cst<float>(k1);
+    c.out[0] = st<float>(p->s[0]);
+    c.out[1] = st<float>(p->s[1]);
+    c.nx = p->nx;
+    c.ny = p->ny;
+    c.shift = 1;
+    c.scale = 1.0f;
+    e = sgpe::launch_copy<float>(c, s);
+  } else {
+    sgpe::CopyArgs<double> c{};
+    c.in[0] = cst<double>(k0);
+    c.in[1] = cst<double>(k1);
+    c.out[0] = st<double>(p->s[0]);
+    c.out[1] = st<double>(p->s[1]);
+    c.nx = p->nx;
+    c.ny = p->ny;
+    c.shift = 1;
+    c.scale = 1.0;
+    e = sgpe::launch_copy<double>(c, s);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "load_psik");
+  p->form = kKspace;
+  p->pending_pops = nullptr;
+  return SGPE_OK;
+}
+
+int sgpe_store_psik(sgpe_plan* p, void* o0, void* o1, double* pops, void* stream) {
+  if (p == nullptr || o0 == nullptr || o1 == nullptr) return fail(SGPE_ERR_ARG, "null plan or psik pointer");
+  if (p->form == kEmpty) return fail(SGPE_ERR_STATE, "no state loaded");
+  DeviceGuard g(p->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return p->bits == 64 ? store<float>(p, o0, o1, pops, s) : store<double>(p, o0, o1, pops, s);
+}
+
+int sgpe_single_step(sgpe_plan* p, int sub, void* stream) {
+  if (p == nullptr) return fail(SGPE_ERR_ARG, "null plan");
+  if (sub != 0 && sub != 1) return fail(SGPE_ERR_ARG, "sub must be 0 (outer) or 1 (inner)");
+  if (p->form == kEmpty) return fail(SGPE_ERR_STATE, "no state loaded");
+  if (!ready(p)) return fail(SGPE_ERR_STATE, "physics or sub-step operators not set");
+  DeviceGuard g(p->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return p->bits == 64 ? substep<float>(p, sub, nullptr, s) : substep<double>(p, sub, nullptr, s);
+}
+
+int sgpe_full_steps(sgpe_plan* p, int n_steps, double* pops, void* stream) {
+  if (p == nullptr) return fail(SGPE_ERR_ARG, "null plan");
+  if (n_steps < 0) return fail(SGPE_ERR_ARG, "n_steps must be non-negative");
+  if (p->form == kEmpty) return fail(SGPE_ERR_STATE, "no state loaded");
+  if (!ready(p)) return fail(SGPE_ERR_STATE, "physics or sub-step operators not set");
+  DeviceGuard g(p->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  for (int i = 0; i < n_steps; ++i) {
+    double* slot = (pops != nullptr && i > 0) ? pops + 2 * (i - 1) : nullptr;
+    int rc;
+    if (p->bits == 64) {
+      rc = substep<float>(p, 0, slot, s);
+      if (rc == SGPE_OK) rc = substep<float>(p, 1, nullptr, s);
+      if (rc == SGPE_OK) rc = substep<float>(p, 0, nullptr, s);
+    } else {
+      rc = substep<double>(p, 0, slot, s);
+      if (rc == SGPE_OK) rc = substep<double>(p, 1, nullptr, s);
+      if (rc == SGPE_OK) rc = substep<double>(p, 0, nullptr, s);
+    }
+    if (rc != SGPE_OK) return rc;
+  }
+  if (pops != nullptr && n_steps > 0) p->pending_pops = pops + 2 * (n_steps - 1);
+  return SGPE_OK;
+}
+
+int sgpe_time_passes(sgpe_plan* p, int n_steps, double* col_ms, double* row_ms, void* stream) {
+  if (p == nullptr || col_ms == nullptr || row_ms == nullptr || n_steps < 1)
+    return fail(SGPE_ERR_ARG, "null plan/outputs or n_steps < 1");
+  if (p->form == kEmpty) return fail(SGPE_ERR_STATE, "no state loaded");
+  if (!ready(p)) return fail(SGPE_ERR_STATE, "physics or sub-step operators not set");
+  DeviceGuard g(p->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int n_pass = 3 * n_steps;
+  std::vector<cudaEvent_t> ev(4 * n_pass, nullptr);
+  cudaError_t e = cudaSuccess;
+  for (auto& x : ev)
+    if (e == cudaSuccess) e = cudaEventCreate(&x);
+  for (int i = 0; i < n_pass && e == cudaSuccess; ++i) {
+    const int sub = (i % 3 == 1) ? 1 : 0;
+    e = cudaEventRecord(ev[4 * i + 0], s);
+    if (e == cudaSuccess) e = p->bits == 64 ? col_pass_step<float>(p, sub, s) : col_pass_step<double>(p, sub, s);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[4 * i + 1], s);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[4 * i + 2], s);
+    if (e == cudaSuccess)
+      e = p->bits == 64 ? row_pass_step<float>(p, sub, nullptr, s) : row_pass_step<double>(p, sub, nullptr, s);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[4 * i + 3], s);
+    if (e == cudaSuccess) {
+      p->form = kMixed;
+      p->prev_sub = sub;
+    }
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  double tc = 0.0, tr = 0.0;
+  for (int i = 0; i < n_pass && e == cudaSuccess; ++i) {
+    float a = 0.f, b = 0.f;
+    e = cudaEventElapsedTime(&a, ev[4 * i + 0], ev[4 * i + 1]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&b, ev[4 * i + 2], ev[4 * i + 3]);
+    tc += a;
+    tr += b;
+  }
+  for (auto& x : ev)
+    if (x) cudaEventDestroy(x);
+  if (e != cudaSuccess) return cuda_fail(e, "time_passes");
+  p->pending_pops = nullptr;
+  *col_ms = tc / n_pass;
+  *row_ms = tr / n_pass;
+  return SGPE_OK;
+}
+
+int sgpe_fft2(sgpe_plan* p, const void* i0, const void* i1, void* o0, void* o1, int inverse, double scale,
+              void* stream) {
+  if (p == nullptr || !i0 || !i1 || !o0 || !o1) return fail(SGPE_ERR_ARG, "null plan or data pointer");
+  DeviceGuard g(p->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return p->bits == 64 ? fft2<float>(p, i0, i1, o0, o1, inverse, scale, s)
+                       : fft2<double>(p, i0, i1, o0, o1, inverse, scale, s);
+}
+
+}  // extern "C"

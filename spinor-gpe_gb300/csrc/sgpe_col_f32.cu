@@ -1,0 +1,7 @@
+// Column-pass kernels, complex64: explicit instantiation.
+#define SGPE_INSTANTIATE
+#include "sgpe_launch.cuh"
+
+namespace sgpe {
+template cudaError_t launch_col<float>(const ColArgs<float>&, int, cudaStream_t);
+}  // namespace sgpe

@@ -1,0 +1,225 @@
+// Register/shared-memory FFT engine for the split-step solver (sm_103a).
+//
+// A line of N complex points is held by T = N/E threads, E points each.
+// Thread j holds the points at positions j + m*T (m = 0..E-1) both before
+// and after a transform: the Stockham autosort stages below are arranged so
+// that the first stage reads straight from registers and the last stage
+// writes straight back to registers, with (stages - 1) exchanges through
+// shared memory in between.  Loads and stores of a line are therefore
+// coalesced (consecutive threads hold consecutive points for each m) and the
+// output is in natural order, which lets a kernel apply point-wise operators
+// between an inverse and a forward transform without any reordering.
+//
+// Stage s has radix R_s (E, E, ..., remainder) and sub-length Ns = prod of
+// the earlier radices.  A thread runs Q = E/R_s butterflies per stage on the
+// "virtual threads" vt = j + q*T; inputs are at vt + r*N/R, twiddle
+// W_N^{(vt mod Ns) * r * N/(Ns*R)}, outputs at (vt/Ns)*Ns*R + vt mod Ns + r*Ns.
+//
+// Twiddles come from a table W_N^i = exp(-2 pi i i/N) computed in FP64 on the
+// host and rounded once to the working precision.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sgpe {
+
+template <typename R> struct CxT;
+template <> struct CxT<float> { using type = float2; };
+template <> struct CxT<double> { using type = double2; };
+template <typename R> using Cx = typename CxT<R>::type;
+
+__device__ __forceinline__ float fmadd(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fmadd(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+template <class C> __device__ __forceinline__ C cmake(decltype(C::x) a, decltype(C::x) b) {
+  C r; r.x = a; r.y = b; return r;
+}
+template <class C> __device__ __forceinline__ C cadd(C a, C b) { return cmake<C>(a.x + b.x, a.y + b.y); }
+template <class C> __device__ __forceinline__ C csub(C a, C b) { return cmake<C>(a.x - b.x, a.y - b.y); }
+template <class C> __device__ __forceinline__ C cmul(C a, C b) {
+  return cmake<C>(fmadd(a.x, b.x, -a.y * b.y), fmadd(a.x, b.y, a.y * b.x));
+}
+// a * conj(b)
+template <class C> __device__ __forceinline__ C cmulc(C a, C b) {
+  return cmake<C>(fmadd(a.x, b.x, a.y * b.y), fmadd(a.y, b.x, -a.x * b.y));
+}
+template <class C> __device__ __forceinline__ C cscale(C a, decltype(C::x) s) { return cmake<C>(a.x * s, a.y * s); }
+template <class C> __device__ __forceinline__ decltype(C::x) cabs2(C a) { return fmadd(a.x, a.x, a.y * a.y); }
+// a * (DIR * i): DIR = -1 gives a * (-i), DIR = +1 gives a * i
+template <int DIR, class C> __device__ __forceinline__ C crot(C a) {
+  return DIR < 0 ? cmake<C>(a.y, -a.x) : cmake<C>(-a.y, a.x);
+}
+// multiply by the twiddle factor exp(DIR * 2 pi i m / 16), m a compile-time constant
+template <int DIR, int M, class C> __device__ __forceinline__ C tw16(C a) {
+  using R = decltype(C::x);
+  constexpr int m = M & 15;
+  const R c1 = R(0.92387953251128675613);  // cos(pi/8)
+  const R s1 = R(0.38268343236508977173);  // sin(pi/8)
+  const R h = R(0.70710678118654752440);   // sqrt(1/2)
+  const R d = R(DIR);
+  if constexpr (m == 0) return a;
+  else if constexpr (m == 4) return crot<DIR>(a);
+  else if constexpr (m == 8) return cmake<C>(-a.x, -a.y);
+  else if constexpr (m == 12) return crot<-DIR>(a);
+  else if constexpr (m == 2) return cscale(cmake<C>(a.x - d * a.y, a.y + d * a.x), h);
+  else if constexpr (m == 6) return cscale(cmake<C>(-a.x - d * a.y, d * a.x - a.y), h);
+  else if constexpr (m == 1) return cmul(a, cmake<C>(c1, d * s1));
+  else if constexpr (m == 3) return cmul(a, cmake<C>(s1, d * c1));
+  else if constexpr (m == 9) return cmul(a, cmake<C>(-c1, -d * s1));
+  else {
+    static_assert(m == 1 || m == 2 || m == 3 || m == 6 || m == 9, "unused twiddle");
+    return a;
+  }
+}
+
+// In-register DFT of size R in natural order: a[k] <- sum_n a[n] exp(DIR 2 pi i nk/R)
+template <int R, int DIR> struct Dft;
+
+template <int DIR> struct Dft<1, DIR> {
+  template <class C> __device__ __forceinline__ static void run(C*) {}
+};
+template <int DIR> struct Dft<2, DIR> {
+  template <class C> __device__ __forceinline__ static void run(C* a) {
+    C t = a[0];
+    a[0] = cadd(t, a[1]);
+    a[1] = csub(t, a[1]);
+  }
+};
+template <int DIR> struct Dft<4, DIR> {
+  template <class C> __device__ __forceinline__ static void run(C* a) {
+    C t0 = cadd(a[0], a[2]), t1 = csub(a[0], a[2]);
+    C t2 = cadd(a[1], a[3]), t3 = crot<DIR>(csub(a[1], a[3]));
+    a[0] = cadd(t0, t2);
+    a[2] = csub(t0, t2);
+    a[1] = cadd(t1, t3);
+    a[3] = csub(t1, t3);
+  }
+};
+template <int DIR> struct Dft<8, DIR> {
+  template <class C> __device__ __forceinline__ static void run(C* a) {
+    C e[4] = {a[0], a[2], a[4], a[6]};
+    C o[4] = {a[1], a[3], a[5], a[7]};
+    Dft<4, DIR>::run(e);
+    Dft<4, DIR>::run(o);
+    o[1] = tw16<DIR, 2>(o[1]);
+    o[2] = tw16<DIR, 4>(o[2]);
+    o[3] = tw16<DIR, 6>(o[3]);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      a[k] = cadd(e[k], o[k]);
+      a[k + 4] = csub(e[k], o[k]);
+    }
+  }
+};
+template <int DIR> struct Dft<16, DIR> {
+  template <class C> __device__ __forceinline__ static void run(C* a) {
+    // n = n2 + 4 n1, k = k1 + 4 k2: inner DFT4 over n1, twiddle W16^{n2 k1},
+    // outer DFT4 over n2.
+    C b[16];
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) {
+      C t[4] = {a[n2], a[n2 + 4], a[n2 + 8], a[n2 + 12]};
+      Dft<4, DIR>::run(t);
+#pragma unroll
+      for (int k1 = 0; k1 < 4; ++k1) b[4 * k1 + n2] = t[k1];
+    }
+    b[4 * 1 + 1] = tw16<DIR, 1>(b[4 * 1 + 1]);
+    b[4 * 1 + 2] = tw16<DIR, 2>(b[4 * 1 + 2]);
+    b[4 * 1 + 3] = tw16<DIR, 3>(b[4 * 1 + 3]);
+    b[4 * 2 + 1] = tw16<DIR, 2>(b[4 * 2 + 1]);
+    b[4 * 2 + 2] = tw16<DIR, 4>(b[4 * 2 + 2]);
+    b[4 * 2 + 3] = tw16<DIR, 6>(b[4 * 2 + 3]);
+    b[4 * 3 + 1] = tw16<DIR, 3>(b[4 * 3 + 1]);
+    b[4 * 3 + 2] = tw16<DIR, 6>(b[4 * 3 + 2]);
+    b[4 * 3 + 3] = tw16<DIR, 9>(b[4 * 3 + 3]);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+      C t[4] = {b[4 * k1 + 0], b[4 * k1 + 1], b[4 * k1 + 2], b[4 * k1 + 3]};
+      Dft<4, DIR>::run(t);
+#pragma unroll
+      for (int k2 = 0; k2 < 4; ++k2) a[k1 + 4 * k2] = t[k2];
+    }
+  }
+};
+
+// Shared-memory view used by the exchange stages: element i of line l of the
+// calling thread's group lives at base[l * line_stride + i + i / E] (one pad
+// element per E elements keeps the radix-E scatter free of bank conflicts).
+template <class C, int E> struct LineSmem {
+  C* base;
+  int line_stride;
+  __device__ __forceinline__ C ld(int l, int i) const { return base[l * line_stride + i + i / E]; }
+  __device__ __forceinline__ void st(int l, int i, C v) const { base[l * line_stride + i + i / E] = v; }
+  __device__ __forceinline__ void sync() const { __syncthreads(); }
+};
+
+// One Stockham stage (and, recursively, the stages after it) on L lines.
+template <int N, int E, int DIR, int L, int NS, class C, class SM>
+__device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, const C* __restrict__ tw) {
+  constexpr int T = N / E;
+  constexpr int R = (N / NS < E) ? (N / NS) : E;
+  constexpr int Q = E / R;
+  constexpr bool kFirst = (NS == 1);
+  constexpr bool kLast = (NS * R == N);
+  static_assert(E % R == 0, "radix must divide the points per thread");
+  C a[L][Q][R];
+#pragma unroll
+  for (int l = 0; l < L; ++l)
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if constexpr (kFirst) a[l][q][r] = v[l][q + r * Q];
+        else a[l][q][r] = sm.ld(l, j + q * T + r * (N / R));
+      }
+  if constexpr (!kFirst) {
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int vt = j + q * T;
+      const int step = (vt % NS) * (N / (NS * R));
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        const C w = __ldg(tw + step * r);
+#pragma unroll
+        for (int l = 0; l < L; ++l) a[l][q][r] = (DIR < 0) ? cmul(a[l][q][r], w) : cmulc(a[l][q][r], w);
+      }
+    }
+  }
+#pragma unroll
+  for (int l = 0; l < L; ++l)
+#pragma unroll
+    for (int q = 0; q < Q; ++q) Dft<R, DIR>::run(a[l][q]);
+  if constexpr (kLast) {
+#pragma unroll
+    for (int l = 0; l < L; ++l)
+#pragma unroll
+      for (int q = 0; q < Q; ++q)
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[l][q + r * Q] = a[l][q][r];
+  } else {
+    sm.sync();  // earlier readers of the exchange buffer are done
+#pragma unroll
+    for (int l = 0; l < L; ++l)
+#pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        const int vt = j + q * T;
+        const int base = (vt / NS) * NS * R + (vt % NS);
+#pragma unroll
+        for (int r = 0; r < R; ++r) sm.st(l, base + r * NS, a[l][q][r]);
+      }
+    sm.sync();
+    fft_stage<N, E, DIR, L, NS * R>(v, j, sm, tw);
+  }
+}
+
+// Transform L lines of length N held as described above.  DIR = -1 is the
+// unnormalised forward DFT (exp(-2 pi i kn/N)), DIR = +1 the unnormalised
+// inverse.  Every thread of the block must call this the same number of
+// times (it synchronises the block between stages).
+template <int N, int E, int DIR, int L, class C, class SM>
+__device__ __forceinline__ void fft_lines(C (&v)[L][E], int j, const SM& sm, const C* __restrict__ tw) {
+  static_assert(N % E == 0, "N must be a multiple of E");
+  fft_stage<N, E, DIR, L, 1>(v, j, sm, tw);
+}
+
+}  // namespace sgpe

@@ -1,0 +1,349 @@
+"""Drop-in ``TensorPropagator``: the spinor-gpe split-step propagator backed
+by the native GB300 kernels.
+
+Same constructor, methods and readable attributes as the original
+(``spinor_gpe/pspinor/tensor_propagator.py:67-324``).  The time stepping runs
+entirely in ``libspinor_gb300.so``: two fused sweeps over the state per
+Strang sub-step, renormalisation and populations reduced on the device, no
+host synchronisation inside a step loop.  There is no CPU path: a ``device``
+that is not a CUDA device raises.
+
+Differences a caller can observe:
+
+* ``device`` defaults to ``'cuda'``; ``dtype`` (64 or 128, default 128) selects
+  complex64 or complex128 arithmetic.
+* ``psik`` is materialised on read from the device state (functional, as in
+  the original, which rebinds ``self.psik`` every sub-step); assigning it loads
+  a new state.
+* ``eng_out`` / ``eng_in`` are dicts whose ``'kin'``, ``'pot'`` and ``'coupl'``
+  entries are built on first access; ``single_step`` accepts only these two
+  dicts.
+* ``eng_expect`` evaluates the original's energy convention
+  (``tensor_propagator.py:273-324``) with a spectral kinetic term instead of
+  finite differences of the unwrapped phase (scikit-image is not used).
+"""
+import numpy as np
+import torch
+
+from . import _native
+from . import operators as ops
+from . import prop_result
+from . import tensor_tools as ttools
+from .plotting_tools import next_available_path
+
+try:  # progress bar as in the original; optional
+    from tqdm import tqdm as _tqdm
+except ImportError:  # pragma: no cover
+    def _tqdm(it, **_):
+        return it
+
+MAGIC_GAMMA = 1 / (2 + 2**(1 / 3))     # tensor_propagator.py:101
+
+
+def _bits(dtype):
+    if dtype in (64, 'complex64', torch.complex64, np.complex64):
+        return 64
+    if dtype in (128, 'complex128', torch.complex128, np.complex128):
+        return 128
+    raise ValueError(f'dtype must be complex64 or complex128, got {dtype!r}')
+
+
+def cuda_device(device):
+    """torch.device for a CUDA device string; raises for anything else."""
+    dev = torch.device(device)
+    if dev.type != 'cuda':
+        raise ValueError(
+            f"device {device!r}: this propagator runs only on CUDA devices "
+            "(the split step is implemented by the native GB300 kernels and "
+            "has no CPU fallback); pass device='cuda'.")
+    if not torch.cuda.is_available():
+        raise RuntimeError('CUDA is not available in this process')
+    if dev.index is None:
+        dev = torch.device('cuda', torch.cuda.current_device())
+    return dev
+
+
+class SubstepOperators(dict):
+    """``eng_out`` / ``eng_in``: the operators of one sub-step.
+
+    ``sub`` is 0 (outer) or 1 (inner).  The dense ``'kin'``, ``'pot'`` and
+    ``'coupl'`` tensors of the original (tensor_propagator.py:138-149) are
+    built from the FP64 specs on first access.
+    """
+
+    def __init__(self, owner, sub, spec):
+        super().__init__()
+        self.owner = owner
+        self.sub = sub
+        self.spec = spec
+
+    def __missing__(self, key):
+        p = self.owner
+        ny, nx = p._shape
+        cdt = p._ctype
+        dev = p._device
+
+        def dense(fa, fb=None):
+            v = fa.dense(ny, nx)
+            if fb is not None:
+                v = v * fb.dense(ny, nx)
+            return torch.as_tensor(v, dtype=cdt, device=dev)
+        s = self.spec
+        if key == 'kin':   # centred k order, like the original
+            val = [torch.as_tensor(np.fft.fftshift(
+                s.kin_a[c].dense(ny, nx) * s.kin_b[c].dense(ny, nx)),
+                dtype=cdt, device=dev) for c in range(2)]
+        elif key == 'pot':
+            val = [dense(s.pot_a[c], s.pot_b[c]) for c in range(2)]
+        elif key == 'coupl':
+            cc, cs, ce = (s.cpl_c.dense(ny, nx), s.cpl_s.dense(ny, nx),
+                          s.cpl_e.dense(ny, nx))
+            val = [[torch.as_tensor(cc, dtype=cdt, device=dev),
+                    torch.as_tensor(cs * np.conj(ce), dtype=cdt, device=dev)],
+                   [torch.as_tensor(cs * ce, dtype=cdt, device=dev),
+                    torch.as_tensor(cc, dtype=cdt, device=dev)]]
+        else:
+            raise KeyError(key)
+        self[key] = val
+        return val
+
+
+class TensorPropagator:
+    """GPU propagator of the pseudospin-1/2 GPE (see the module docstring).
+
+    Parameters follow ``tensor_propagator.py:67-91``: ``spin`` (a
+    ``PSpinor``), ``t_step``, ``n_steps``, ``device``, ``time`` ('imag' or
+    'real'), ``is_sampling``, ``n_samples``; plus ``dtype`` (64 / 128).
+    """
+
+    # pylint: disable=too-many-instance-attributes
+    def __init__(self, spin, t_step, n_steps, device='cuda', time='imag',
+                 is_sampling=False, n_samples=1, dtype=128):
+        self.n_steps = n_steps
+        self._device = cuda_device(device)
+        self.device = device
+        self.paths = spin.paths
+
+        if time == 'imag':
+            self.t_step = -1.0j * t_step
+        elif time == 'real':
+            self.t_step = t_step
+        else:
+            raise ValueError("time must be 'imag' or 'real'")
+        self.time = time
+        self.dt_out = self.t_step * MAGIC_GAMMA
+        self.dt_in = self.t_step * (1 - 2 * MAGIC_GAMMA)
+
+        self.rand_seed = spin.rand_seed
+        if self.rand_seed is not None:
+            torch.manual_seed(self.rand_seed)
+        self.is_sampling = is_sampling
+
+        self.atom_num = spin.atom_num
+        self.is_coupling = spin.is_coupling
+        self.g_sc = spin.g_sc
+        self._bits = _bits(dtype)
+        self._ctype = torch.complex64 if self._bits == 64 else torch.complex128
+        self._rtype = torch.float32 if self._bits == 64 else torch.float64
+
+        self._kin_np = [np.asarray(k, dtype=np.float64)
+                        for k in spin.kin_eng_spin]
+        self._pot_np = [np.asarray(v, dtype=np.float64)
+                        for v in spin.pot_eng_spin]
+        self._coupling_np = np.asarray(spin.coupling, dtype=np.float64)
+        psik0 = [np.asarray(p) for p in spin.psik]
+        self._shape = psik0[0].shape
+        ny, nx = self._shape
+        keys_space = ['dr', 'dk', 'x_mesh', 'y_mesh', 'dv_r', 'dv_k']
+        self._space_np = {k: np.asarray(spin.space[k]) for k in keys_space}
+        self._kx_np = np.asarray(spin.space['kx_mesh']) \
+            if 'kx_mesh' in spin.space else None
+        self._ky_np = np.asarray(spin.space['ky_mesh']) \
+            if 'ky_mesh' in spin.space else None
+        self.space = {k: torch.tensor(v, device=self._device)
+                      for k, v in self._space_np.items()}
+
+        # pylint: disable=invalid-name
+        self.kL_recoil = spin.kL_recoil
+        self.rot_coupling = spin.rot_coupling
+        if spin.rot_coupling:                     # tensor_propagator.py:125-129
+            self._expon_np = None
+            self.expon = torch.tensor(0.0)
+        else:
+            self._expon_np = 2 * self.kL_recoil * self._space_np['x_mesh']
+            self.expon = torch.as_tensor(self._expon_np, device=self._device)
+
+        if self.is_sampling:
+            assert self.n_steps % n_samples == 0, (
+                f"The number of samples requested {n_samples} does not evenly "
+                f"divide the total number of steps {self.n_steps}.")
+        self.sample_rate = self.n_steps / n_samples
+
+        self._plan = _native.Plan(ny, nx, self._bits, self._device.index)
+        dv_r = float(self._space_np['dv_r'])
+        dv_k = float(self._space_np['dv_k'])
+        self._plan.set_physics(float(self.g_sc['uu']), float(self.g_sc['dd']),
+                               float(self.g_sc['ud']), float(self.atom_num),
+                               dv_r, dv_k, self.is_coupling)
+        spec_out = ops.build_substep(self.dt_out, self._kin_np, self._pot_np,
+                                     self._coupling_np, self._expon_np, True)
+        spec_in = ops.build_substep(self.dt_in, self._kin_np, self._pot_np,
+                                    self._coupling_np, self._expon_np, False)
+        self._plan.set_substep(0, spec_out)
+        self._plan.set_substep(1, spec_in)
+        self.eng_out = SubstepOperators(self, 0, spec_out)
+        self.eng_in = SubstepOperators(self, 1, spec_in)
+        self._psik_cache = None
+        self.psik = [torch.as_tensor(p, dtype=self._ctype, device=self._device)
+                     for p in psik0]
+
+    # ------------------------------------------------------------ attributes
+    @property
+    def kin_eng_spin(self):
+        """Kinetic energy grids as device tensors (tensor_propagator.py:114)."""
+        return [torch.as_tensor(k, device=self._device) for k in self._kin_np]
+
+    @property
+    def pot_eng_spin(self):
+        """Potential energy grids as device tensors (tensor_propagator.py:116)."""
+        return [torch.as_tensor(v, device=self._device) for v in self._pot_np]
+
+    @property
+    def coupling(self):
+        return torch.as_tensor(self._coupling_np, device=self._device)
+
+    @property
+    def psik(self):
+        """The current k-space spinor: two device tensors, centred k order,
+        renormalised to the atom number (tensor_propagator.py:271)."""
+        if self._psik_cache is None:
+            ny, nx = self._shape
+            out = [torch.empty((ny, nx), dtype=self._ctype,
+                               device=self._device) for _ in range(2)]
+            self._plan.store_psik(torch, out)
+            self._psik_cache = out
+        return self._psik_cache
+
+    @psik.setter
+    def psik(self, value):
+        psik = [torch.as_tensor(p, device=self._device).to(self._ctype)
+                .contiguous() for p in value]
+        if len(psik) != 2 or psik[0].shape != self._shape:
+            raise ValueError(f'psik must be two {self._shape} arrays')
+        self._plan.load_psik(torch, psik)
+        self._psik_cache = [p.clone() for p in psik]
+
+    # ------------------------------------------------------------- stepping
+    def full_step(self):
+        """Outer, inner, outer sub-steps (tensor_propagator.py:214-222)."""
+        self._plan.full_steps(torch, 1, self._device)
+        self._psik_cache = None
+
+    def single_step(self, t_step, eng):
+        """One Strang sub-step (tensor_propagator.py:224-271).  ``eng`` must
+        be ``self.eng_out`` or ``self.eng_in`` (with their ``t_step``)."""
+        if eng is self.eng_out:
+            sub, expected = 0, self.dt_out
+        elif eng is self.eng_in:
+            sub, expected = 1, self.dt_in
+        else:
+            raise ValueError('single_step accepts only the eng_out / eng_in '
+                             'operators of this propagator')
+        if not np.isclose(complex(t_step), complex(expected), rtol=1e-12,
+                          atol=0.0):
+            raise ValueError('t_step does not match the operators passed')
+        self._plan.single_step(torch, sub, self._device)
+        self._psik_cache = None
+
+    def full_steps(self, n_steps, pops=None):
+        """``n_steps`` full steps in one call; ``pops`` is an optional
+        (n_steps, 2) float64 device tensor receiving the populations after
+        each step (the last row is filled when the state is next read)."""
+        if pops is not None:
+            if (pops.dtype != torch.float64 or pops.device != self._device
+                    or tuple(pops.shape) != (n_steps, 2)
+                    or not pops.is_contiguous()):
+                raise ValueError('pops must be a contiguous (n_steps, 2) '
+                                 'float64 tensor on the propagator device')
+        self._plan.full_steps(torch, n_steps, self._device, pops)
+        self._psik_cache = None
+
+    def prop_loop(self, n_steps):
+        """Propagate ``n_steps`` full steps; record populations every step and
+        optionally sample psik (tensor_propagator.py:151-212)."""
+        pop_times = np.linspace(0, self.n_steps * np.abs(self.t_step),
+                                n_steps)
+        pops = {'times': pop_times, 'vals': np.empty((n_steps, 2))}
+        pops_dev = torch.empty((max(n_steps, 1), 2), dtype=torch.float64,
+                               device=self._device)
+        if self.is_sampling:
+            n_samples = int(n_steps / self.sample_rate)
+            ny, nx = self._shape
+            sampled_psik = np.empty((n_samples, 2, ny, nx),
+                                    dtype=np.complex128)
+            sampled_times = np.linspace(0, self.n_steps * np.abs(self.t_step),
+                                        n_samples)
+            rate = int(self.sample_rate)
+            bounds = list(range(0, n_steps, rate)) + [n_steps]
+        else:
+            chunk = max(1, min(n_steps, 200))
+            bounds = list(range(0, n_steps, chunk)) + [n_steps]
+        bar = _tqdm(range(len(bounds) - 1), disable=len(bounds) < 3)
+        for b in bar:
+            i0, i1 = bounds[b], bounds[b + 1]
+            if self.is_sampling:
+                idx = i0 // rate
+                sampled_psik[idx] = np.array(ttools.to_numpy(self.psik))
+            if i1 > i0:
+                self.full_steps(i1 - i0, pops_dev[i0:i1])
+        psik_t = self.psik                  # also fills the last pops row
+        pops['vals'][:] = pops_dev[:n_steps].cpu().numpy()
+        energy = self.eng_expect(psik_t)
+
+        if self.is_sampling:
+            test_name = self.paths['trial'] + 'psik_sampled'
+            file_name = next_available_path(test_name, self.paths['folder'],
+                                            '.npz')
+            np.savez(file_name, psiks=sampled_psik, times=sampled_times)
+        else:
+            file_name = None
+
+        psik = ttools.to_numpy(psik_t)
+        psi = ttools.to_numpy(ttools.ifft_2d(psik_t, self._space_np['dr']))
+        return prop_result.PropResult(psi, psik, energy, pops, file_name)
+
+    # --------------------------------------------------------------- energy
+    def eng_expect(self, psik):
+        """[E_tot, E_kin, E_pot, E_int] in the convention of
+        ``tensor_propagator.py:273-324`` (grid sums without the area
+        element).  The kinetic term
+        sum(|grad sqrt(n)|^2 + n |grad phi|^2 + 2 kL n d_x phi) / 2 is
+        evaluated spectrally as sum_k ((kx^2+ky^2)/2 + kL kx) |psik|^2 dv_k / dv_r
+        (the kL term only with coupling), which needs no phase unwrapping."""
+        assert len(psik) == 2, ("Requires two spinor components to calculate "
+                                "the energy expectation value.")
+        if isinstance(psik[0], np.ndarray):
+            psik = [torch.as_tensor(p, device=self._device).to(self._ctype)
+                    for p in psik]
+        dv_r = float(self._space_np['dv_r'])
+        dv_k = float(self._space_np['dv_k'])
+        f64 = torch.float64
+        kx = torch.as_tensor(self._kx_np, dtype=f64, device=self._device)
+        ky = torch.as_tensor(self._ky_np, dtype=f64, device=self._device)
+        kin_density = (kx**2 + ky**2) / 2
+        if self.is_coupling:
+            kin_density = kin_density + self.kL_recoil * kx
+        densk = [(torch.abs(p)**2).to(f64) for p in psik]
+        kin = float(sum((kin_density * d).sum() for d in densk)) * dv_k / dv_r
+        psi = ttools.ifft_2d(psik, self._space_np['dr'])
+        dens = [(torch.abs(p)**2).to(f64) for p in psi]
+        pot = float(sum((torch.as_tensor(v, device=self._device) * d).sum()
+                        for v, d in zip(self._pot_np, dens)))
+        g = self.g_sc
+        int_e = float((g['uu'] * dens[0]**2 + g['dd'] * dens[1]**2
+                       + g['ud'] * dens[0] * dens[1]).sum())
+        cross = (torch.conj(psi[0]) * psi[1]).to(torch.complex128)
+        coupl = float((2 * cross.real * torch.as_tensor(
+            self._coupling_np, device=self._device) / 2).sum())
+        total = kin + pot + int_e + coupl
+        return [total, kin, pot, int_e]

@@ -1,0 +1,250 @@
+"""Parity of the native GPU path with the original propagator.
+
+Every check runs the drop-in ``TensorPropagator`` / ``tensor_tools`` (which
+call the C ABI of ``libspinor_gb300.so``) and compares with the golden
+vectors of the original package or with the pinned CPU oracle on the same
+inputs.
+
+Tolerances (relative L2 over both components, against the complex128
+reference): 1e-10 for complex128 runs, 1e-5 for complex64 runs.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import case_params, load_cases, rel_l2, spin_from_case
+from oracle import OraclePropagator, OracleInputs, calc_pops
+
+pytestmark = pytest.mark.gpu
+
+TOL = {128: 1e-10, 64: 1e-5}
+CASES = load_cases()
+PROP_CASES = sorted(k for k in CASES if k != 'fft')
+
+
+@pytest.fixture(scope='module')
+def tp():
+    assert torch.cuda.is_available(), 'these tests need a CUDA device'
+    from spinor_gpe.pspinor import tensor_propagator
+    return tensor_propagator
+
+
+def _c128_twin(name):
+    """Golden complex128 case with the same inputs as a complex64 case."""
+    return CASES[name[:-4]] if name.endswith('_c64') else CASES[name]
+
+
+@pytest.mark.parametrize('name', PROP_CASES)
+def test_single_step_matches_reference(tp, tmp_path, name):
+    case = CASES[name]
+    p = case_params(case)
+    prop = tp.TensorPropagator(spin_from_case(case, tmp_path), p['dt'],
+                               p['n_steps'], 'cuda', time=p['time'],
+                               dtype=p['dtype'])
+    prop.single_step(prop.dt_out, prop.eng_out)
+    got = np.array([t.cpu().numpy() for t in prop.psik])
+    ref = _c128_twin(name)['psik_single_out']
+    assert rel_l2(got, ref) <= TOL[p['dtype']]
+
+
+@pytest.mark.parametrize('name', PROP_CASES)
+def test_full_steps_and_pops_match_reference(tp, tmp_path, name):
+    case = CASES[name]
+    p = case_params(case)
+    prop = tp.TensorPropagator(spin_from_case(case, tmp_path), p['dt'],
+                               p['n_steps'], 'cuda', time=p['time'],
+                               dtype=p['dtype'])
+    prop.full_step()
+    got1 = np.array([t.cpu().numpy() for t in prop.psik])
+    twin = _c128_twin(name)
+    assert rel_l2(got1, twin['psik_step1']) <= TOL[p['dtype']]
+    n = p['n_steps'] - 1
+    pops = torch.empty((n, 2), dtype=torch.float64, device='cuda')
+    prop.full_steps(n, pops)
+    got = np.array([t.cpu().numpy() for t in prop.psik])
+    assert rel_l2(got, twin['psik_final']) <= TOL[p['dtype']]
+    ptol = 1e-12 if p['dtype'] == 128 else 1e-6
+    np.testing.assert_allclose(pops.cpu().numpy(), twin['pops'][1:],
+                               rtol=0, atol=ptol)
+
+
+def test_complex64_tracks_reference_complex64(tp, tmp_path):
+    """The complex64 run is as close to the original's own complex64 run as
+    both are to complex128."""
+    for name in ['imag_plain_32_c64', 'real_raman_32_c64']:
+        case = CASES[name]
+        p = case_params(case)
+        prop = tp.TensorPropagator(spin_from_case(case, tmp_path), p['dt'],
+                                   p['n_steps'], 'cuda', time=p['time'],
+                                   dtype=64)
+        prop.full_steps(p['n_steps'])
+        got = np.array([t.cpu().numpy() for t in prop.psik])
+        assert rel_l2(got, case['psik_final']) <= 1e-5
+
+
+def _oracle_run(inputs, dt, time, n_steps, dtype=128):
+    orc = OraclePropagator(inputs, dt, time, dtype)
+    pops = orc.run(n_steps)
+    return orc.psik_numpy(), pops
+
+
+def _inputs_from_spin(ps):
+    return OracleInputs(
+        psik=[np.asarray(p) for p in ps.psik],
+        kin_eng_spin=[np.asarray(k) for k in ps.kin_eng_spin],
+        pot_eng_spin=[np.asarray(v) for v in ps.pot_eng_spin],
+        coupling=np.asarray(ps.coupling, dtype=np.float64),
+        x_mesh=ps.space['x_mesh'], dr=ps.space['dr'],
+        dv_r=float(ps.space['dv_r']), dv_k=float(ps.space['dv_k']),
+        g_sc=dict(ps.g_sc), atom_num=float(ps.atom_num),
+        kL_recoil=float(ps.kL_recoil), rot_coupling=bool(ps.rot_coupling),
+        is_coupling=bool(ps.is_coupling))
+
+
+@pytest.mark.parametrize('dtype', [128, 64])
+def test_ground_state_256_against_oracle(tp, tmp_path, dtype):
+    """256^2 plain ground state (complex128 in its problem statement)."""
+    from spinor_gpe import workloads
+    from spinor_gpe.pspinor import pspinor as spin
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    ps = workloads.ground_state_256(spin.PSpinor, ttools.fft_2d,
+                                    str(tmp_path / 'c1') + '/')
+    n = 20
+    ref_psik, ref_pops = _oracle_run(_inputs_from_spin(ps), 0.02, 'imag', n)
+    prop = tp.TensorPropagator(ps, 0.02, n, 'cuda', time='imag', dtype=dtype)
+    pops = torch.empty((n, 2), dtype=torch.float64, device='cuda')
+    prop.full_steps(n, pops)
+    got = np.array([t.cpu().numpy() for t in prop.psik])
+    assert rel_l2(got, ref_psik) <= TOL[dtype]
+    np.testing.assert_allclose(pops.cpu().numpy(), ref_pops, rtol=0,
+                               atol=1e-12 if dtype == 128 else 1e-6)
+
+
+def test_raman_quench_1024_complex64_against_oracle(tp, tmp_path):
+    """1024^2 complex64 real-time Raman-coupled steps against complex128."""
+    from spinor_gpe import workloads
+    from spinor_gpe.pspinor import pspinor as spin
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    ps = workloads.raman_quench_1024(spin.PSpinor, ttools.fft_2d,
+                                     str(tmp_path / 'c2') + '/', delta=0.5)
+    n = 4
+    ref_psik, ref_pops = _oracle_run(_inputs_from_spin(ps), 1e-3, 'real', n)
+    prop = tp.TensorPropagator(ps, 1e-3, n, 'cuda', time='real', dtype=64)
+    pops = torch.empty((n, 2), dtype=torch.float64, device='cuda')
+    prop.full_steps(n, pops)
+    got = np.array([t.cpu().numpy() for t in prop.psik])
+    assert rel_l2(got, ref_psik) <= 1e-5
+    np.testing.assert_allclose(pops.cpu().numpy(), ref_pops, rtol=0,
+                               atol=1e-6)
+
+
+@pytest.mark.parametrize('shape', [(32, 32), (64, 128), (256, 32),
+                                   (512, 512), (128, 2048), (4096, 64)])
+@pytest.mark.parametrize('dtype', [torch.complex64, torch.complex128])
+def test_fft_2d_matches_numpy(shape, dtype):
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    rng = np.random.default_rng(7)
+    a = [rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+         for _ in range(2)]
+    dr = (0.125, 0.25)
+    ref_k = ttools.fft_2d(a, dr)           # NumPy on the host
+    ref_r = ttools.ifft_2d(a, dr)
+    t = [torch.as_tensor(x, dtype=dtype, device='cuda') for x in a]
+    got_k = [x.cpu().numpy() for x in ttools.fft_2d(t, dr)]
+    got_r = [x.cpu().numpy() for x in ttools.ifft_2d(t, dr)]
+    tol = 1e-14 if dtype == torch.complex128 else 2e-6
+    assert rel_l2(got_k, ref_k) <= tol
+    assert rel_l2(got_r, ref_r) <= tol
+
+
+@pytest.mark.parametrize('n', [128, 256, 512, 1024])
+def test_fft_invariants_on_gpu(n):
+    """The original's FFT test invariants on all-ones grids
+    (spinor_gpe/tests/fft_func_tests.py: round trip, atom number, Parseval;
+    10 eps)."""
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    eps = torch.finfo(torch.complex128).eps * 10
+    for shape in [(n, n), (n, 128), (128, n)]:
+        grid = [torch.ones(shape, dtype=torch.complex128, device='cuda')] * 2
+        grid_k = ttools.fft_2d(grid, (1, 1))
+        grid_r = ttools.ifft_2d(grid_k, (1, 1))
+        for g, r in zip(grid, grid_r):
+            assert float(torch.max(torch.abs(r - g))) <= eps
+        npts = shape[0] * shape[1]
+        atoms = ttools.calc_atoms(grid)
+        assert abs(atoms - ttools.calc_atoms(grid_r)) <= eps * npts
+        vol = 4 * np.pi**2 / npts
+        assert abs(atoms - ttools.calc_atoms(grid_k, vol)) <= eps * npts
+
+
+def test_prop_loop_api(tmp_path):
+    """imaginary() then real() through PSpinor, with sampling: the
+    PropResult contract (prop_result.py:50-82) and the sampled npz format
+    (tensor_propagator.py:198-204)."""
+    from spinor_gpe import workloads
+    from spinor_gpe.pspinor import pspinor as spin
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    ps = workloads.build(spin.PSpinor, ttools.fft_2d, str(tmp_path / 'loop') + '/',
+                         nx=64, ny=64, half_x=8.0, half_y=8.0,
+                         g=(300.0, 298.0, 296.0), omega=0.7, k_l=3.0,
+                         rot_coupling=False, seed=5)
+    inp = _inputs_from_spin(ps)
+    res, prop = ps.imaginary(0.01, 10, 'cuda', is_sampling=True, n_samples=5)
+    ref_psik, ref_pops = _oracle_run(inp, 0.01, 'imag', 10)
+    assert rel_l2(res.psik, ref_psik) <= 1e-10
+    np.testing.assert_allclose(res.pops['vals'], ref_pops, rtol=0, atol=1e-12)
+    assert res.pops['times'].shape == (10,)
+    assert np.allclose(res.pops['vals'].sum(axis=1), 1.0)
+    assert len(res.eng_final) == 4 and np.isfinite(res.eng_final).all()
+    assert res.psi[0].shape == (64, 64) and len(res.dens) == 2
+    np.testing.assert_allclose(ps.psik[0], res.psik[0])
+    data = np.load(res.sampled_path)
+    assert data['psiks'].shape == (5, 2, 64, 64)
+    assert data['times'].shape == (5,)
+    # chained real-time run after a detuning change (examples/3_raman_rabi.py)
+    ps.detuning_uniform(0.3)
+    inp2 = _inputs_from_spin(ps)
+    res2, _ = ps.real(1e-3, 6, 'cuda')
+    ref2, _ = _oracle_run(inp2, 1e-3, 'real', 6)
+    assert rel_l2(res2.psik, ref2) <= 1e-10
+
+
+def test_psik_setter_and_cpu_rejection(tp, tmp_path):
+    case = CASES['imag_plain_32']
+    spin = spin_from_case(case, tmp_path)
+    with pytest.raises(ValueError):
+        tp.TensorPropagator(spin, 0.02, 1, 'cpu')
+    prop = tp.TensorPropagator(spin, 0.02, 1, 'cuda')
+    before = [t.clone() for t in prop.psik]
+    np.testing.assert_array_equal(before[0].cpu().numpy(), case['psik0'][0])
+    prop.full_step()
+    prop.psik = before
+    prop.full_step()
+    got = np.array([t.cpu().numpy() for t in prop.psik])
+    assert rel_l2(got, case['psik_step1']) <= 1e-10
+    with pytest.raises(ValueError):
+        prop.single_step(prop.dt_in, prop.eng_out)
+
+
+@pytest.mark.parametrize('shape', [(2048, 2048), (32, 4096), (4096, 32)])
+def test_large_and_extreme_shapes_conserve_norm(tp, tmp_path, shape):
+    """Real-time steps at the size limits: atom number before renormalisation
+    stays 1 to complex64 rounding, and the state stays finite."""
+    from spinor_gpe import workloads
+    from spinor_gpe.pspinor import pspinor as spin
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    ny, nx = shape
+    ps = workloads.build(spin.PSpinor, ttools.fft_2d, str(tmp_path / 'x') + '/',
+                         nx=nx, ny=ny, half_x=nx * 0.0625 / 2,
+                         half_y=ny * 0.0625 / 2, g=(100.0, 100.0, 99.0),
+                         omega=1.0, k_l=3.0, delta=0.2, seed=3)
+    prop = tp.TensorPropagator(ps, 1e-3, 3, 'cuda', time='real', dtype=64)
+    pops = torch.empty((3, 2), dtype=torch.float64, device='cuda')
+    prop.full_steps(3, pops)
+    psik = prop.psik
+    assert all(torch.isfinite(p).all() for p in psik)
+    np.testing.assert_allclose(pops.cpu().numpy().sum(axis=1), 1.0,
+                               atol=1e-9)
+    assert abs(sum(calc_pops(psik, float(ps.space['dv_k']))) - 1.0) < 1e-5

@@ -116,6 +116,9 @@ int sgpe_single_step(sgpe_plan* plan, int sub, void* stream);
  * sgpe_store_psik with pops_dev = NULL, or the first sub-step of the next
  * sgpe_single_step / sgpe_full_steps), so pops_dev must stay valid until
  * then.  sgpe_load_psik discards that pending write.
+ * Without populations, steady-state steps are replayed from CUDA graphs the
+ * plan captures on first use (one graph launch per 8 steps); changing the
+ * physics or operators discards them.
  * Replaces: TensorPropagator.full_step (tensor_propagator.py:214-222) and the
  * step loop of prop_loop (:185-194). */
 int sgpe_full_steps(sgpe_plan* plan, int n_steps, double* pops_dev, void* stream);
@@ -130,9 +133,11 @@ int sgpe_fft2(sgpe_plan* plan, const void* in0, const void* in1, void* out0, voi
               int inverse, double scale, void* stream);
 
 /* Measurement helper: n_steps full steps exactly as sgpe_full_steps (no
- * populations), with CUDA events recorded on `stream` around every column
- * pass and every row pass.  Synchronises the stream and returns the mean
- * duration of one column pass and of one row pass in milliseconds.
+ * populations), captured into a CUDA graph with events around every column
+ * pass and every row pass, launched once on `stream`.  Synchronises the
+ * stream and returns the mean device duration of one column pass and of one
+ * row pass in milliseconds.  Advances the state by n_steps steps (plus at
+ * most one step to reach the graph's steady state).
  * Instrumentation of the native path; no counterpart in the original. */
 int sgpe_time_passes(sgpe_plan* plan, int n_steps, double* col_ms, double* row_ms, void* stream);
 

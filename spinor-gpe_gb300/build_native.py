@@ -48,20 +48,29 @@ def _stale(lib, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force=False, verbose=False, extra_flags=()):
+def build(force=False, verbose=False, extra_flags=(), lib_path=None,
+          build_dir=None, reuse_objects=()):
     """Compile and link the library; returns its path.  Skips the work when
-    the library is newer than every source and header."""
+    the library is newer than every source and header.  ``lib_path`` /
+    ``build_dir`` redirect the outputs (tuning builds); object files named in
+    ``reuse_objects`` (basenames without .o) are linked from ``build_dir``
+    as they are instead of being recompiled."""
+    lib = lib_path or LIB
+    bdir = build_dir or BUILD
     srcs = _sources()
     deps = srcs + [os.path.join(CSRC, f) for f in os.listdir(CSRC)
                    if f.endswith('.cuh')]
     deps.append(os.path.join(INCLUDE, 'spinor_gb300.h'))
-    if not force and not extra_flags and not _stale(LIB, deps):
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
+    if not force and not extra_flags and not _stale(lib, deps):
+        return lib
+    os.makedirs(bdir, exist_ok=True)
     nvcc = _nvcc()
 
     def compile_one(src):
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + '.o')
+        name = os.path.basename(src)[:-3]
+        obj = os.path.join(bdir, name + '.o')
+        if name in reuse_objects and os.path.exists(obj):
+            return obj
         cmd = [nvcc, *ARCH, *FLAGS, *extra_flags, '-c', src, '-o', obj]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
@@ -72,13 +81,13 @@ def build(force=False, verbose=False, extra_flags=()):
 
     with ThreadPoolExecutor(max_workers=len(srcs)) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = LIB + '.tmp'
+    tmp = lib + '.tmp'
     cmd = [nvcc, *ARCH, '-shared', '-o', tmp, *objs]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f'link failed:\n{res.stderr}')
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == '__main__':

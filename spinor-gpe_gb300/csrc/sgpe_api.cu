@@ -8,8 +8,10 @@
 //                                        row pass; see sgpe_kernels.cuh)
 // store_psik materialises psik from MIXED (column pass + renormalisation)
 // without changing the state.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -35,21 +37,46 @@ struct DevField {
   int sx = 0, sy = 0;
 };
 
+// FP64 host copy of a field (kept for the kinetic factors, which are
+// combined pairwise into the merged tables of the fused column pass).
+struct HostField {
+  std::vector<double> v;  // interleaved (re, im)
+  int sx = 0, sy = 0;
+};
+
 struct SubOps {
   DevField kin_a[2], kin_b[2], pot_a[2], pot_b[2], cc, cs, ce;
+  HostField kin_host[2][2];  // [comp][a, b]
   double zr = 0.0, zi = 0.0;
+  std::vector<void*> allocs;
+  bool set = false;
+};
+
+// Kinetic factors of two consecutive sub-steps multiplied together in FP64
+// (exp(-i K t_prev/2) exp(-i K t_next/2)) and rounded once: one table pass
+// in the column kernel instead of two.
+struct PairOps {
+  DevField a[2], b[2];
   std::vector<void*> allocs;
   bool set = false;
 };
 
 enum Form { kEmpty = 0, kKspace = 1, kMixed = 2 };
 
-// Restores the caller's current device on scope exit.
+// Makes `dev` current and restores the caller's device on scope exit (no
+// driver call when it is already current).
 struct DeviceGuard {
   int prev = -1;
   bool ok = false;
   explicit DeviceGuard(int dev) {
-    if (cudaGetDevice(&prev) == cudaSuccess && cudaSetDevice(dev) == cudaSuccess) ok = true;
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess) return;
+    if (cur == dev) {
+      ok = true;
+    } else if (cudaSetDevice(dev) == cudaSuccess) {
+      prev = cur;
+      ok = true;
+    }
   }
   ~DeviceGuard() {
     if (prev >= 0) cudaSetDevice(prev);
@@ -68,6 +95,7 @@ struct sgpe_plan {
   void* tw_x = nullptr;
   void* tw_y = nullptr;
   SubOps sub[2];
+  PairOps pair[2][2];        // [prev][next]
   double g[3] = {0, 0, 0};
   double atom_num = 1.0, dv_r = 1.0, dv_k = 1.0;
   int coupling = 0;
@@ -77,23 +105,47 @@ struct sgpe_plan {
   // Device slot that receives the populations of the current (mixed) state
   // when they are next computed: set by sgpe_full_steps for its last step.
   double* pending_pops = nullptr;
+  // CUDA graphs of steady-state full steps (mixed form, previous sub-step
+  // outer, no populations): the six launches of a step have fixed arguments,
+  // so one graph launch replaces them.  graph[0]: 1 step, graph[1]: kGraphSteps.
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  bool graphs_enabled = true;
 };
 
 namespace {
+constexpr int kGraphSteps = 8;
+}
 
-template <typename R> void* upload_twiddles(int n, cudaError_t* err) {
+namespace {
+
+// Per-stage twiddle table of an (n, e) transform, in the order the FFT
+// engine reads it (sgpe_fft.cuh: tw_offset): for each stage (ns, r_s),
+// entries exp(-2 pi i k r / (ns r_s)) at (r - 1) * ns + k.  Angles are
+// reduced exactly in integers and evaluated in FP64, then rounded once.
+template <typename R> void* upload_twiddles(int n, int e, cudaError_t* err) {
   using C = sgpe::Cx<R>;
-  std::vector<C> h(n);
+  std::vector<C> h;
   const double two_pi = 6.283185307179586476925286766559;
-  for (int i = 0; i < n; ++i) {
-    const double ang = two_pi * double(i) / double(n);
-    h[i].x = R(std::cos(ang));
-    h[i].y = R(-std::sin(ang));
+  for (int ns = 1; ns < n;) {
+    const int rs = (n / ns < e) ? n / ns : e;
+    const long long len = (long long)ns * rs;
+    for (int r = 1; r < rs; ++r)
+      for (int k = 0; k < ns; ++k) {
+        const long long m = ((long long)k * r) % len;
+        const double ang = two_pi * double(m) / double(len);
+        C c;
+        c.x = R(std::cos(ang));
+        c.y = R(-std::sin(ang));
+        h.push_back(c);
+      }
+    ns *= rs;
   }
+  if (h.empty()) h.push_back(C{R(1), R(0)});
   void* d = nullptr;
-  *err = cudaMalloc(&d, sizeof(C) * n);
+  *err = cudaMalloc(&d, sizeof(C) * h.size());
   if (*err != cudaSuccess) return nullptr;
-  *err = cudaMemcpy(d, h.data(), sizeof(C) * n, cudaMemcpyHostToDevice);
+  *err = cudaMemcpy(d, h.data(), sizeof(C) * h.size(), cudaMemcpyHostToDevice);
   return d;
 }
 
@@ -125,6 +177,76 @@ int upload_field(sgpe_plan* p, const sgpe_field& f, DevField* out, SubOps* so, c
   return SGPE_OK;
 }
 
+int upload_host_field(sgpe_plan* p, const HostField& hf, DevField* out, std::vector<void*>* allocs) {
+  sgpe_field f;
+  f.data = hf.v.data();
+  f.n = int(hf.v.size() / 2);
+  f.sx = hf.sx;
+  f.sy = hf.sy;
+  SubOps tmp;
+  int rc = upload_field(p, f, out, &tmp, "merged kinetic");
+  for (void* q : tmp.allocs) allocs->push_back(q);
+  tmp.allocs.clear();
+  return rc;
+}
+
+// Element-wise product of two broadcast fields, evaluated in FP64.
+HostField multiply_fields(const HostField& fa, const HostField& fb, int nx, int ny) {
+  HostField r;
+  if (fa.sx == fb.sx && fa.sy == fb.sy) {
+    r.sx = fa.sx;
+    r.sy = fa.sy;
+  } else if (fa.sx == 0 && fa.sy == 0) {
+    r.sx = fb.sx;
+    r.sy = fb.sy;
+  } else if (fb.sx == 0 && fb.sy == 0) {
+    r.sx = fa.sx;
+    r.sy = fa.sy;
+  } else {
+    r.sx = 1;
+    r.sy = nx;
+  }
+  const int xs = r.sx ? nx : 1, ys = r.sy ? ny : 1;
+  long long n = 0;
+  for (int y = 0; y < ys; ++y)
+    for (int x = 0; x < xs; ++x) n = std::max(n, (long long)x * r.sx + (long long)y * r.sy + 1);
+  r.v.assign(2 * n, 0.0);
+  for (int y = 0; y < ys; ++y)
+    for (int x = 0; x < xs; ++x) {
+      const long long ia = (long long)x * fa.sx + (long long)y * fa.sy;
+      const long long ib = (long long)x * fb.sx + (long long)y * fb.sy;
+      const long long ir = (long long)x * r.sx + (long long)y * r.sy;
+      const double ar = fa.v[2 * ia], ai = fa.v[2 * ia + 1];
+      const double br = fb.v[2 * ib], bi = fb.v[2 * ib + 1];
+      r.v[2 * ir] = ar * br - ai * bi;
+      r.v[2 * ir + 1] = ar * bi + ai * br;
+    }
+  return r;
+}
+
+void free_pair(PairOps& po) {
+  for (void* q : po.allocs) cudaFree(q);
+  po = PairOps();
+}
+
+// Merged kinetic tables for (prev, next), built on first use.
+int ensure_pair(sgpe_plan* p, int prev, int next) {
+  PairOps& po = p->pair[prev][next];
+  if (po.set) return SGPE_OK;
+  for (int c = 0; c < 2; ++c) {
+    const HostField ma = multiply_fields(p->sub[prev].kin_host[c][0], p->sub[next].kin_host[c][0], p->nx, p->ny);
+    const HostField mb = multiply_fields(p->sub[prev].kin_host[c][1], p->sub[next].kin_host[c][1], p->nx, p->ny);
+    int rc = upload_host_field(p, ma, &po.a[c], &po.allocs);
+    if (rc == SGPE_OK) rc = upload_host_field(p, mb, &po.b[c], &po.allocs);
+    if (rc != SGPE_OK) {
+      free_pair(po);
+      return rc;
+    }
+  }
+  po.set = true;
+  return SGPE_OK;
+}
+
 template <typename R> sgpe::Field<R> typed(const DevField& f) {
   return sgpe::Field<R>{static_cast<const sgpe::Cx<R>*>(f.p), f.sx, f.sy};
 }
@@ -134,6 +256,15 @@ template <typename R> sgpe::KinOp<R> kin_op(const SubOps& so) {
   for (int c = 0; c < 2; ++c) {
     k.a[c] = typed<R>(so.kin_a[c]);
     k.b[c] = typed<R>(so.kin_b[c]);
+  }
+  return k;
+}
+
+template <typename R> sgpe::KinOp<R> kin_pair(const PairOps& po) {
+  sgpe::KinOp<R> k;
+  for (int c = 0; c < 2; ++c) {
+    k.a[c] = typed<R>(po.a[c]);
+    k.b[c] = typed<R>(po.b[c]);
   }
   return k;
 }
@@ -156,7 +287,10 @@ template <typename R> sgpe::Cx<R>* st(void* p) { return static_cast<sgpe::Cx<R>*
 template <typename R> const sgpe::Cx<R>* cst(const void* p) { return static_cast<const sgpe::Cx<R>*>(p); }
 
 // Column pass over the state (in place) ending a sub-step and starting `sub`.
-template <typename R> cudaError_t col_pass_step(sgpe_plan* p, int sub, cudaStream_t s) {
+// want_u: the populations of the state entering the pass are needed, so the
+// two kinetic half steps are applied separately (sum after the first).
+template <typename R> cudaError_t col_pass_step(sgpe_plan* p, int sub, double* pops, cudaStream_t s) {
+  const bool want_u = pops != nullptr;
   sgpe::ColArgs<R> a{};
   a.in[0] = cst<R>(p->s[0]);
   a.in[1] = cst<R>(p->s[1]);
@@ -166,10 +300,18 @@ template <typename R> cudaError_t col_pass_step(sgpe_plan* p, int sub, cudaStrea
   a.nx = p->nx;
   a.fwd = (p->form == kMixed);
   a.inv = 1;
-  a.has_kprev = (p->form == kMixed);
-  if (a.has_kprev) a.kprev = kin_op<R>(p->sub[p->prev_sub]);
-  a.has_knext = 1;
-  a.knext = kin_op<R>(p->sub[sub]);
+  if (p->form != kMixed) {
+    a.nk = 1;
+    a.k1 = kin_op<R>(p->sub[sub]);
+  } else if (want_u) {
+    a.nk = 2;
+    a.k1 = kin_op<R>(p->sub[p->prev_sub]);
+    a.k2 = kin_op<R>(p->sub[sub]);
+  } else {
+    if (ensure_pair(p, p->prev_sub, sub) != SGPE_OK) return cudaErrorMemoryAllocation;
+    a.nk = 1;
+    a.k1 = kin_pair<R>(p->pair[p->prev_sub][sub]);
+  }
   a.scale = R(1);
   a.part = p->part;
   return sgpe::launch_col<R>(a, p->ny, s);
@@ -201,7 +343,7 @@ template <typename R> int substep(sgpe_plan* p, int sub, double* pops, cudaStrea
   const bool fused = (p->form == kMixed);
   if (fused && pops == nullptr) pops = p->pending_pops;
   p->pending_pops = nullptr;
-  cudaError_t e = col_pass_step<R>(p, sub, s);
+  cudaError_t e = col_pass_step<R>(p, sub, fused ? pops : nullptr, s);
   if (e != cudaSuccess) return cuda_fail(e, "column pass");
   e = row_pass_step<R>(p, sub, fused ? pops : nullptr, s);
   if (e != cudaSuccess) return cuda_fail(e, "row pass");
@@ -234,9 +376,8 @@ template <typename R> int store(sgpe_plan* p, void* o0, void* o1, double* pops, 
   a.fwd = 1;
   a.inv = 0;
   a.out_shift = 1;
-  a.has_kprev = 1;
-  a.kprev = kin_op<R>(p->sub[p->prev_sub]);
-  a.has_knext = 0;
+  a.nk = 1;
+  a.k1 = kin_op<R>(p->sub[p->prev_sub]);
   a.scale = R(1);
   a.part = p->part;
   cudaError_t e = sgpe::launch_col<R>(a, p->ny, s);
@@ -269,7 +410,6 @@ template <typename R> int fft2(sgpe_plan* p, const void* i0, const void* i1, voi
   c.tw = cst<R>(p->tw_y);
   c.nx = p->nx;
   c.scale = R(1);
-  c.part = nullptr;
   cudaError_t e;
   if (!inverse) {
     r.in[0] = cst<R>(i0);
@@ -312,6 +452,74 @@ template <typename R> int fft2(sgpe_plan* p, const void* i0, const void* i1, voi
 
 bool ready(sgpe_plan* p) { return p->physics && p->sub[0].set && p->sub[1].set; }
 
+void drop_graphs(sgpe_plan* p) {
+  for (auto& g : p->graph) {
+    if (g) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+}
+
+// One eager full step (outer, inner, outer).
+template <typename R> int eager_step(sgpe_plan* p, double* pops, cudaStream_t s) {
+  int rc = substep<R>(p, 0, pops, s);
+  if (rc == SGPE_OK) rc = substep<R>(p, 1, nullptr, s);
+  if (rc == SGPE_OK) rc = substep<R>(p, 0, nullptr, s);
+  return rc;
+}
+
+// Capture `steps` steady-state full steps into an executable graph.  The plan
+// must be in mixed form after an outer sub-step with no pending populations;
+// the capture leaves that state unchanged.
+template <typename R> int capture_steps(sgpe_plan* p, int steps, cudaGraphExec_t* out) {
+  if (p->cap_stream == nullptr) {
+    cudaError_t e = cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(e, "graph stream");
+  }
+  // merged kinetic tables must exist before capture (they allocate)
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b)
+      if (ensure_pair(p, a, b) != SGPE_OK) return SGPE_ERR_OOM;
+  cudaError_t e = cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return cuda_fail(e, "begin capture");
+  int rc = SGPE_OK;
+  for (int i = 0; i < steps && rc == SGPE_OK; ++i) rc = eager_step<R>(p, nullptr, p->cap_stream);
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(p->cap_stream, &graph);
+  if (rc != SGPE_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "end capture");
+  e = cudaGraphInstantiate(out, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
+  return SGPE_OK;
+}
+
+template <typename R> int full_steps_impl(sgpe_plan* p, int n_steps, double* pops, cudaStream_t s) {
+  int i = 0;
+  while (i < n_steps) {
+    double* slot = (pops != nullptr && i > 0) ? pops + 2 * (i - 1) : nullptr;
+    const bool steady = p->graphs_enabled && slot == nullptr && p->pending_pops == nullptr &&
+                        p->form == kMixed && p->prev_sub == 0 && (pops == nullptr || i > 0);
+    if (steady && pops == nullptr) {
+      const int k = (n_steps - i >= kGraphSteps) ? 1 : 0;
+      if (p->graph[k] == nullptr) {
+        const int rc = capture_steps<R>(p, k ? kGraphSteps : 1, &p->graph[k]);
+        if (rc != SGPE_OK) return rc;
+      }
+      const cudaError_t e = cudaGraphLaunch(p->graph[k], s);
+      if (e != cudaSuccess) return cuda_fail(e, "graph launch");
+      i += k ? kGraphSteps : 1;
+      continue;
+    }
+    const int rc = eager_step<R>(p, slot, s);
+    if (rc != SGPE_OK) return rc;
+    ++i;
+  }
+  return SGPE_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -335,6 +543,9 @@ int sgpe_plan_create(sgpe_plan** out, int ny, int nx, int dtype_bits, int device
   p->bits = dtype_bits;
   p->device = device;
   p->elem = dtype_bits == 64 ? sizeof(float2) : sizeof(double2);
+  // SGPE_DISABLE_GRAPHS (any value) makes this plan launch every step
+  // eagerly; used to check graph replay against eager launches.
+  p->graphs_enabled = std::getenv("SGPE_DISABLE_GRAPHS") == nullptr;
   const int cols = dtype_bits == 64 ? sgpe::col_tile_width<float>(ny) : sgpe::col_tile_width<double>(ny);
   if (cols == 0 || nx % cols != 0 || (nx / 2) % cols != 0) {
     delete p;
@@ -343,15 +554,16 @@ int sgpe_plan_create(sgpe_plan** out, int ny, int nx, int dtype_bits, int device
   p->ntile = nx / cols;
   cudaError_t e = cudaSuccess;
   for (int c = 0; c < 2 && e == cudaSuccess; ++c) e = cudaMalloc(&p->s[c], p->elem * (size_t)nx * ny);
-  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&p->part), sizeof(double) * 4 * p->ntile);
-  if (e == cudaSuccess) e = cudaMemset(p->part, 0, sizeof(double) * 4 * p->ntile);
+  const size_t red_bytes = sizeof(double) * 4 * (size_t)p->ntile;
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&p->part), red_bytes);
+  if (e == cudaSuccess) e = cudaMemset(p->part, 0, red_bytes);
   if (e == cudaSuccess) {
     if (dtype_bits == 64) {
-      p->tw_x = upload_twiddles<float>(nx, &e);
-      if (e == cudaSuccess) p->tw_y = upload_twiddles<float>(ny, &e);
+      p->tw_x = upload_twiddles<float>(nx, sgpe::row_points_per_thread<float>(nx), &e);
+      if (e == cudaSuccess) p->tw_y = upload_twiddles<float>(ny, sgpe::col_points_per_thread<float>(ny), &e);
     } else {
-      p->tw_x = upload_twiddles<double>(nx, &e);
-      if (e == cudaSuccess) p->tw_y = upload_twiddles<double>(ny, &e);
+      p->tw_x = upload_twiddles<double>(nx, sgpe::row_points_per_thread<double>(nx), &e);
+      if (e == cudaSuccess) p->tw_y = upload_twiddles<double>(ny, sgpe::col_points_per_thread<double>(ny), &e);
     }
   }
   if (e != cudaSuccess) {
@@ -365,6 +577,8 @@ int sgpe_plan_create(sgpe_plan** out, int ny, int nx, int dtype_bits, int device
 int sgpe_plan_destroy(sgpe_plan* p) {
   if (p == nullptr) return SGPE_OK;
   DeviceGuard g(p->device);
+  drop_graphs(p);
+  if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   for (int c = 0; c < 2; ++c) {
     if (p->s[c]) cudaFree(p->s[c]);
     if (p->scratch[c]) cudaFree(p->scratch[c]);
@@ -374,6 +588,8 @@ int sgpe_plan_destroy(sgpe_plan* p) {
   if (p->tw_y) cudaFree(p->tw_y);
   free_sub(p->sub[0]);
   free_sub(p->sub[1]);
+  for (int i = 0; i < 2; ++i)
+    for (int k = 0; k < 2; ++k) free_pair(p->pair[i][k]);
   delete p;
   return SGPE_OK;
 }
@@ -391,6 +607,7 @@ int sgpe_set_physics(sgpe_plan* p, double g_uu, double g_dd, double g_ud, double
   p->dv_k = dv_k;
   p->coupling = is_coupling ? 1 : 0;
   p->physics = true;
+  drop_graphs(p);
   return SGPE_OK;
 }
 
@@ -414,11 +631,24 @@ int sgpe_set_substep(sgpe_plan* p, int sub, const sgpe_substep_ops* ops) {
     free_sub(so);
     return rc;
   }
+  for (int c = 0; c < 2; ++c) {
+    const sgpe_field* src[2] = {&ops->kin_a[c], &ops->kin_b[c]};
+    for (int k = 0; k < 2; ++k) {
+      so.kin_host[c][k].v.assign(src[k]->data, src[k]->data + 2 * (size_t)src[k]->n);
+      so.kin_host[c][k].sx = src[k]->sx;
+      so.kin_host[c][k].sy = src[k]->sy;
+    }
+  }
   so.zr = ops->int_z_re;
   so.zi = ops->int_z_im;
   so.set = true;
   free_sub(p->sub[sub]);
   p->sub[sub] = std::move(so);
+  drop_graphs(p);
+  for (int i = 0; i < 2; ++i) {
+    free_pair(p->pair[sub][i]);
+    free_pair(p->pair[i][sub]);
+  }
   return SGPE_OK;
 }
 
@@ -481,20 +711,9 @@ int sgpe_full_steps(sgpe_plan* p, int n_steps, double* pops, void* stream) {
   if (!ready(p)) return fail(SGPE_ERR_STATE, "physics or sub-step operators not set");
   DeviceGuard g(p->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  for (int i = 0; i < n_steps; ++i) {
-    double* slot = (pops != nullptr && i > 0) ? pops + 2 * (i - 1) : nullptr;
-    int rc;
-    if (p->bits == 64) {
-      rc = substep<float>(p, 0, slot, s);
-      if (rc == SGPE_OK) rc = substep<float>(p, 1, nullptr, s);
-      if (rc == SGPE_OK) rc = substep<float>(p, 0, nullptr, s);
-    } else {
-      rc = substep<double>(p, 0, slot, s);
-      if (rc == SGPE_OK) rc = substep<double>(p, 1, nullptr, s);
-      if (rc == SGPE_OK) rc = substep<double>(p, 0, nullptr, s);
-    }
-    if (rc != SGPE_OK) return rc;
-  }
+  const int rc = p->bits == 64 ? full_steps_impl<float>(p, n_steps, pops, s)
+                               : full_steps_impl<double>(p, n_steps, pops, s);
+  if (rc != SGPE_OK) return rc;
   if (pops != nullptr && n_steps > 0) p->pending_pops = pops + 2 * (n_steps - 1);
   return SGPE_OK;
 }
@@ -506,25 +725,49 @@ int sgpe_time_passes(sgpe_plan* p, int n_steps, double* col_ms, double* row_ms, 
   if (!ready(p)) return fail(SGPE_ERR_STATE, "physics or sub-step operators not set");
   DeviceGuard g(p->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // reach the steady state (mixed form after an outer sub-step) eagerly
+  if (!(p->form == kMixed && p->prev_sub == 0 && p->pending_pops == nullptr)) {
+    const int rc = p->bits == 64 ? eager_step<float>(p, nullptr, s) : eager_step<double>(p, nullptr, s);
+    if (rc != SGPE_OK) return rc;
+  }
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b)
+      if (ensure_pair(p, a, b) != SGPE_OK) return SGPE_ERR_OOM;
+  if (p->cap_stream == nullptr) {
+    cudaError_t e = cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(e, "graph stream");
+  }
+  // Capture n_steps steps with timing events around every pass (external
+  // event-record nodes), so that the measured intervals are device time
+  // between back-to-back graph nodes.
   const int n_pass = 3 * n_steps;
   std::vector<cudaEvent_t> ev(4 * n_pass, nullptr);
   cudaError_t e = cudaSuccess;
   for (auto& x : ev)
     if (e == cudaSuccess) e = cudaEventCreate(&x);
-  for (int i = 0; i < n_pass && e == cudaSuccess; ++i) {
-    const int sub = (i % 3 == 1) ? 1 : 0;
-    e = cudaEventRecord(ev[4 * i + 0], s);
-    if (e == cudaSuccess) e = p->bits == 64 ? col_pass_step<float>(p, sub, s) : col_pass_step<double>(p, sub, s);
-    if (e == cudaSuccess) e = cudaEventRecord(ev[4 * i + 1], s);
-    if (e == cudaSuccess) e = cudaEventRecord(ev[4 * i + 2], s);
-    if (e == cudaSuccess)
-      e = p->bits == 64 ? row_pass_step<float>(p, sub, nullptr, s) : row_pass_step<double>(p, sub, nullptr, s);
-    if (e == cudaSuccess) e = cudaEventRecord(ev[4 * i + 3], s);
-    if (e == cudaSuccess) {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t cs = p->cap_stream;
+  if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    for (int i = 0; i < n_pass && e == cudaSuccess; ++i) {
+      const int sub = (i % 3 == 1) ? 1 : 0;
+      e = cudaEventRecordWithFlags(ev[4 * i + 0], cs, cudaEventRecordExternal);
+      if (e == cudaSuccess)
+        e = p->bits == 64 ? col_pass_step<float>(p, sub, nullptr, cs) : col_pass_step<double>(p, sub, nullptr, cs);
+      if (e == cudaSuccess) e = cudaEventRecordWithFlags(ev[4 * i + 1], cs, cudaEventRecordExternal);
+      if (e == cudaSuccess) e = cudaEventRecordWithFlags(ev[4 * i + 2], cs, cudaEventRecordExternal);
+      if (e == cudaSuccess)
+        e = p->bits == 64 ? row_pass_step<float>(p, sub, nullptr, cs) : row_pass_step<double>(p, sub, nullptr, cs);
+      if (e == cudaSuccess) e = cudaEventRecordWithFlags(ev[4 * i + 3], cs, cudaEventRecordExternal);
       p->form = kMixed;
       p->prev_sub = sub;
     }
+    const cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+    if (e == cudaSuccess) e = e2;
   }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (e == cudaSuccess) e = cudaGraphLaunch(exec, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   double tc = 0.0, tr = 0.0;
   for (int i = 0; i < n_pass && e == cudaSuccess; ++i) {
@@ -534,10 +777,11 @@ int sgpe_time_passes(sgpe_plan* p, int n_steps, double* col_ms, double* row_ms, 
     tc += a;
     tr += b;
   }
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
   for (auto& x : ev)
     if (x) cudaEventDestroy(x);
   if (e != cudaSuccess) return cuda_fail(e, "time_passes");
-  p->pending_pops = nullptr;
   *col_ms = tc / n_pass;
   *row_ms = tr / n_pass;
   return SGPE_OK;

@@ -15,8 +15,12 @@
 // "virtual threads" vt = j + q*T; inputs are at vt + r*N/R, twiddle
 // W_N^{(vt mod Ns) * r * N/(Ns*R)}, outputs at (vt/Ns)*Ns*R + vt mod Ns + r*Ns.
 //
-// Twiddles come from a table W_N^i = exp(-2 pi i i/N) computed in FP64 on the
-// host and rounded once to the working precision.
+// Twiddles come from per-stage tables computed in FP64 on the host and rounded
+// once to the working precision: stage (NS, R) uses
+//   T[(r - 1) * NS + k] = exp(-2 pi i k r / (NS R)),  r = 1..R-1, k = 0..NS-1,
+// after the blocks of the earlier stages (tw_offset).  For a fixed r,
+// threads with consecutive k read consecutive entries, so a warp's twiddle
+// loads are coalesced.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -142,6 +146,18 @@ template <int DIR> struct Dft<16, DIR> {
   }
 };
 
+// Offset of the twiddle block of the stage with sub-length NS in the table
+// of an (N, E) transform; tw_offset(N, E, N) is the table length.
+__host__ __device__ constexpr int tw_offset(int N, int E, int NS) {
+  int off = 0, ns = 1;
+  while (ns < NS) {
+    const int r = (N / ns < E) ? N / ns : E;
+    off += (r - 1) * ns;
+    ns *= r;
+  }
+  return off;
+}
+
 // Shared-memory view used by the exchange stages: element i of line l of the
 // calling thread's group lives at base[l * line_stride + i + i / E] (one pad
 // element per E elements keeps the radix-E scatter free of bank conflicts).
@@ -154,7 +170,13 @@ template <class C, int E> struct LineSmem {
 };
 
 // One Stockham stage (and, recursively, the stages after it) on L lines.
-template <int N, int E, int DIR, int L, int NS, class C, class SM>
+// FROM_SMEM: the first stage reads the natural-order line from shared memory
+// instead of registers; TO_SMEM: the last stage writes the natural-order
+// result to shared memory instead of registers.  In both cases a thread
+// touches exactly the positions j + m*T it holds in the register layout, so
+// no barrier is needed between a thread's own point-wise pass over those
+// positions and the adjacent transform.
+template <int N, int E, int DIR, int L, int NS, bool FROM_SMEM, bool TO_SMEM, class C, class SM>
 __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, const C* __restrict__ tw) {
   constexpr int T = N / E;
   constexpr int R = (N / NS < E) ? (N / NS) : E;
@@ -169,17 +191,18 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
     for (int q = 0; q < Q; ++q)
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        if constexpr (kFirst) a[l][q][r] = v[l][q + r * Q];
+        if constexpr (kFirst && !FROM_SMEM) a[l][q][r] = v[l][q + r * Q];
         else a[l][q][r] = sm.ld(l, j + q * T + r * (N / R));
       }
   if constexpr (!kFirst) {
+    constexpr int kOff = tw_offset(N, E, NS);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       const int vt = j + q * T;
-      const int step = (vt % NS) * (N / (NS * R));
+      const C* twq = tw + kOff + (vt % NS);
 #pragma unroll
       for (int r = 1; r < R; ++r) {
-        const C w = __ldg(tw + step * r);
+        const C w = __ldg(twq + (r - 1) * NS);
 #pragma unroll
         for (int l = 0; l < L; ++l) a[l][q][r] = (DIR < 0) ? cmul(a[l][q][r], w) : cmulc(a[l][q][r], w);
       }
@@ -189,7 +212,7 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
   for (int l = 0; l < L; ++l)
 #pragma unroll
     for (int q = 0; q < Q; ++q) Dft<R, DIR>::run(a[l][q]);
-  if constexpr (kLast) {
+  if constexpr (kLast && !TO_SMEM) {
 #pragma unroll
     for (int l = 0; l < L; ++l)
 #pragma unroll
@@ -207,19 +230,25 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
 #pragma unroll
         for (int r = 0; r < R; ++r) sm.st(l, base + r * NS, a[l][q][r]);
       }
-    sm.sync();
-    fft_stage<N, E, DIR, L, NS * R>(v, j, sm, tw);
+    if constexpr (!kLast) {
+      sm.sync();
+      fft_stage<N, E, DIR, L, NS * R, FROM_SMEM, TO_SMEM>(v, j, sm, tw);
+    }
   }
 }
 
 // Transform L lines of length N held as described above.  DIR = -1 is the
 // unnormalised forward DFT (exp(-2 pi i kn/N)), DIR = +1 the unnormalised
 // inverse.  Every thread of the block must call this the same number of
-// times (it synchronises the block between stages).
-template <int N, int E, int DIR, int L, class C, class SM>
+// times (it synchronises the block between stages).  With FROM_SMEM the
+// input is read from the shared-memory view (natural order; the caller must
+// have synchronised after other threads wrote it, unless each thread wrote
+// only its own positions); with TO_SMEM the output is left there in natural
+// order and `v` is not written.
+template <int N, int E, int DIR, int L, bool FROM_SMEM = false, bool TO_SMEM = false, class C, class SM>
 __device__ __forceinline__ void fft_lines(C (&v)[L][E], int j, const SM& sm, const C* __restrict__ tw) {
   static_assert(N % E == 0, "N must be a multiple of E");
-  fft_stage<N, E, DIR, L, 1>(v, j, sm, tw);
+  fft_stage<N, E, DIR, L, 1, FROM_SMEM, TO_SMEM>(v, j, sm, tw);
 }
 
 }  // namespace sgpe

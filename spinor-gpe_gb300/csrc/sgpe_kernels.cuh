@@ -20,11 +20,19 @@
 // joins the end of one sub-step (kinetic half step) and the start of the next.
 //
 // F denotes the unnormalised DFT; constant factors are absorbed by the
-// renormalisation (see RowArgs::norm_num).
+// renormalisation (see ColArgs::norm_num).
 #pragma once
 #include "sgpe_fft.cuh"
 
+// Unroll factor of the row kernel's point-wise loop (small: keeps the code
+// within the instruction cache).
+#ifndef SGPE_OPS_UNROLL
+#define SGPE_OPS_UNROLL 2
+#endif
+
 namespace sgpe {
+
+constexpr int kOpsUnroll = SGPE_OPS_UNROLL;
 
 // A complex operator field with broadcast strides: value(x, y) = p[x*sx + y*sy].
 // sx = sy = 0 is a uniform value, (1, 0) an x-table, (0, 1) a y-table and
@@ -53,43 +61,74 @@ template <typename R> struct RealOp {
   R zr, zi;
 };
 
+// Field slots of RealOp in a fixed order (for the per-row hoisting below).
+enum { kPa0 = 0, kPb0, kPa1, kPb1, kCc, kCs, kCe, kNumRealFields };
+
+template <typename R> __device__ __forceinline__ const Field<R>& real_field(const RealOp<R>& op, int k) {
+  switch (k) {
+    case kPa0: return op.pa[0];
+    case kPb0: return op.pb[0];
+    case kPa1: return op.pa[1];
+    case kPb1: return op.pb[1];
+    case kCc: return op.cc;
+    case kCs: return op.cs;
+    default: return op.ce;
+  }
+}
+
+// The real-space operator values along one row y.  Fields that do not vary
+// along x (uniform values, y-tables) resolve to one address per row, which a
+// warp reads as a single broadcast.
+template <typename R> struct RowFields {
+  const RealOp<R>* op;
+  int y;
+  __device__ __forceinline__ void init(const RealOp<R>& o, int yy) {
+    op = &o;
+    y = yy;
+  }
+  __device__ __forceinline__ Cx<R> at(int k, int x) const { return fld(real_field(*op, k), x, y); }
+};
+
 enum RowMode { kRowStep = 0, kRowForward = 1, kRowInverse = 2 };
 
 template <typename R> struct RowArgs {
   const Cx<R>* in[2];
   Cx<R>* out[2];
-  const Cx<R>* tw;        // W_Nx table
+  const Cx<R>* tw;        // per-stage twiddle table of the x transform
   int mode;               // RowMode
   R scale;                // forward/inverse modes: constant output scale
-  // step mode: renormalisation from the preceding column pass
+  // step mode: renormalisation from the partial sums of the preceding
+  // column pass, lambda = sqrt(norm_num / sum w)
   const double* part;     // [2 comps][ntile][u, w]
   int ntile;
-  double norm_num;        // lambda^2 * sum|w|^2 = atom_num / (Nx Ny dv_r)
+  double norm_num;        // atom_num / (Nx Ny dv_r)
   R g_uu, g_dd, g_ud;
   int coupling;
   RealOp<R> op;
-  double* pops;           // non-null: block 0 writes the populations of the state
-                          // the preceding column pass started from
+  double* pops;           // non-null: block 0 writes the populations of the
+                          // state the preceding column pass started from
   double atom_num;
 };
 
 template <typename R> struct ColArgs {
   const Cx<R>* in[2];
   Cx<R>* out[2];
-  const Cx<R>* tw;        // W_Ny table
+  const Cx<R>* tw;        // per-stage twiddle table of the y transform
   int nx;
   int fwd, inv;           // forward F_y first / inverse F_y^-1 last
   int in_shift, out_shift;  // centred (fftshift) order on input / output
-  int has_kprev, has_knext;
-  KinOp<R> kprev, knext;
+  int nk;                 // kinetic tables applied after F_y: 0, 1 or 2
+  KinOp<R> k1, k2;        // k1 first; u = sum|psik|^2 after k1, w after k2
+                          // (w = u when nk < 2)
   R scale;
-  double* part;           // non-null: per block [u, w] sums
+  double* part;           // non-null: per-block partial sums [comp][tile][u, w]
+                          // (FP64; the consumer of the pass sums them)
 };
 
 template <typename R> struct ScaleArgs {
   Cx<R>* d[2];
   long long n;            // elements per component
-  const double* part;
+  const double* part;     // partials of the column pass that wrote d
   int ntile;
   double atom_num, dv;
   double* pops;
@@ -103,15 +142,34 @@ template <typename R> struct CopyArgs {
   R scale;
 };
 
-__device__ __forceinline__ double warp_sum(double v) {
+// Butterfly (pairwise) sum over a warp.
+template <typename T> __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
-// Sum of |v[m]|^2 over the E points of a thread: pairwise in the working
-// precision, so the per-thread error stays at log2(E) roundings.
-template <int E, class C> __device__ __forceinline__ double thread_norm2(const C (&v)[E]) {
+// Sums of the column-pass partials [2][ntile][u, w] by one warp, in FP64 and
+// a fixed order: (sum u_0, sum u_1, sum w) returned on every lane.
+__device__ __forceinline__ void sum_partials(const double* part, int ntile, int lane, double* u0, double* u1,
+                                             double* w) {
+  double su0 = 0.0, su1 = 0.0, sw = 0.0;
+  for (int i = lane; i < 2 * ntile; i += 32) {
+    const double u = part[2 * i], ww = part[2 * i + 1];
+    sw += ww;
+    if (i < ntile) su0 += u; else su1 += u;
+  }
+  *u0 = warp_sum(su0);
+  *u1 = warp_sum(su1);
+  *w = warp_sum(sw);
+}
+
+// Sum of |v[m]|^2 over the E points of a thread, pairwise in the working
+// precision.  Block sums continue pairwise (warp butterfly, then across
+// warps), so a block partial carries about log2(block points) roundings; only
+// the cross-block sum is FP64.  (FP64 arithmetic runs at a small fraction of
+// the FP32 rate on this GPU, so it is kept out of the per-thread work.)
+template <int E, class C> __device__ __forceinline__ decltype(C::x) thread_norm2(const C (&v)[E]) {
   using R = decltype(C::x);
   R s[E];
 #pragma unroll
@@ -120,7 +178,7 @@ template <int E, class C> __device__ __forceinline__ double thread_norm2(const C
   for (int w = 1; w < E; w <<= 1)
 #pragma unroll
     for (int m = 0; m + w < E; m += 2 * w) s[m] += s[m + w];
-  return double(s[0]);
+  return s[0];
 }
 
 __device__ __forceinline__ void sin_cos(float x, float* s, float* c) { sincosf(x, s, c); }
@@ -128,57 +186,138 @@ __device__ __forceinline__ void sin_cos(double x, double* s, double* c) { sincos
 __device__ __forceinline__ float exp_r(float x) { return expf(x); }
 __device__ __forceinline__ double exp_r(double x) { return exp(x); }
 
-// exp(z * e) for the interaction operator (library expf/sincosf, not the
-// reduced-accuracy intrinsics).
+// sin and cos of an FP32 argument.  For |x| <= pi/4 (always the case for the
+// interaction phases of a stable time step) the Taylor series of sin to x^9
+// and of cos to x^10 in Horner form; the first omitted terms are below
+// 2e-9 (sin, relative) and 1.2e-10 (cos) there, under half an FP32 ulp.
+// Larger arguments use the library sincosf.
+__device__ __forceinline__ void sin_cos_phase(float x, float* s, float* c) {
+  if (fabsf(x) <= 0.78539816f) {
+    const float x2 = x * x;
+    float ps = fmadd(x2, 1.0f / 362880.0f, -1.0f / 5040.0f);
+    ps = fmadd(ps, x2, 1.0f / 120.0f);
+    ps = fmadd(ps, x2, -1.0f / 6.0f);
+    *s = fmadd(ps * x2, x, x);
+    float pc = fmadd(x2, -1.0f / 3628800.0f, 1.0f / 40320.0f);
+    pc = fmadd(pc, x2, -1.0f / 720.0f);
+    pc = fmadd(pc, x2, 1.0f / 24.0f);
+    pc = fmadd(pc, x2, -0.5f);
+    *c = fmadd(pc, x2, 1.0f);
+  } else {
+    sincosf(x, s, c);
+  }
+}
+__device__ __forceinline__ void sin_cos_phase(double x, double* s, double* c) { sincos(x, s, c); }
+
+// exp(z * e) for the interaction operator.
 template <typename R> __device__ __forceinline__ Cx<R> cexp_z(R zr, R zi, R e) {
   using C = Cx<R>;
   if (zi == R(0)) return cmake<C>(exp_r(zr * e), R(0));
   R sn, cs;
-  sin_cos(zi * e, &sn, &cs);
+  sin_cos_phase(zi * e, &sn, &cs);
   if (zr == R(0)) return cmake<C>(cs, sn);
   const R g = exp_r(zr * e);
   return cmake<C>(g * cs, g * sn);
 }
 
+// Real-space operators of one sub-step at one point x of a row, both
+// components (tensor_propagator.py:247-267): interaction, coupling,
+// potential, coupling, and the interaction again with the same operator.
+template <typename R>
+__device__ __forceinline__ void real_space_ops(Cx<R>& p0, Cx<R>& p1, int x, const RowFields<R>& rf,
+                                               const RowArgs<R>& a) {
+  using C = Cx<R>;
+  const RealOp<R>& op = a.op;
+  const R n0 = cabs2(p0), n1 = cabs2(p1);
+  const R e0 = fmadd(a.g_uu, n0, a.g_ud * n1);
+  const R e1 = fmadd(a.g_dd, n1, a.g_ud * n0);
+  const C i0 = cexp_z(op.zr, op.zi, e0);
+  const C i1 = cexp_z(op.zr, op.zi, e1);
+  p0 = cmul(p0, i0);
+  p1 = cmul(p1, i1);
+  C cc, s01, s10;
+  if (a.coupling) {
+    cc = rf.at(kCc, x);
+    const C sv = rf.at(kCs, x), e = rf.at(kCe, x);
+    s01 = cmulc(sv, e);
+    s10 = cmul(sv, e);
+    const C q0 = cadd(cmul(cc, p0), cmul(s01, p1));
+    const C q1 = cadd(cmul(s10, p0), cmul(cc, p1));
+    p0 = q0;
+    p1 = q1;
+  }
+  p0 = cmul(p0, cmul(rf.at(kPa0, x), rf.at(kPb0, x)));
+  p1 = cmul(p1, cmul(rf.at(kPa1, x), rf.at(kPb1, x)));
+  if (a.coupling) {
+    const C q0 = cadd(cmul(cc, p0), cmul(s01, p1));
+    const C q1 = cadd(cmul(s10, p0), cmul(cc, p1));
+    p0 = q0;
+    p1 = q1;
+  }
+  p0 = cmul(p0, i0);
+  p1 = cmul(p1, i1);
+}
+
+// v[m] *= ka(x, ky) * kb(x, ky) for ky = j + m*T along one column x; a
+// factor that does not vary along the column (sy == 0) is loaded once.
+template <typename R, int E, int T>
+__device__ __forceinline__ void apply_kinetic(Cx<R> (&v)[E], const KinOp<R>& k, int comp, int x, int j) {
+  using C = Cx<R>;
+  const Field<R>& fa = k.a[comp];
+  const Field<R>& fb = k.b[comp];
+  const bool a_const = (fa.sy == 0), b_const = (fb.sy == 0);
+  const C a0 = fld(fa, x, j), b0 = fld(fb, x, j);
+#pragma unroll
+  for (int m = 0; m < E; ++m) {
+    const int ky = j + m * T;
+    const C ka = (a_const || m == 0) ? a0 : fld(fa, x, ky);
+    const C kb = (b_const || m == 0) ? b0 : fld(fb, x, ky);
+    v[m] = cmul(v[m], cmul(ka, kb));
+  }
+}
+
 // ----------------------------------------------------------------- row pass
-template <typename R, int N, int E, int ROWS>
-__global__ void __launch_bounds__((N / E) * ROWS)
+// Block: ROWS rows, both components; T = N/E threads per (row, component)
+// line, so 2*T*ROWS threads.  Thread (rho, comp, j) transforms one line; the
+// point-wise operators, which couple the components, run between the
+// transforms on the natural-order rows left in shared memory.
+template <typename R, int N, int E, int ROWS, int MINB>
+__global__ void __launch_bounds__(2 * (N / E) * ROWS, MINB)
 row_kernel(const RowArgs<R> a) {
   using C = Cx<R>;
   constexpr int T = N / E;
   constexpr int LS = N + N / E;
+  constexpr int NT = 2 * T * ROWS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* sm = reinterpret_cast<C*>(smem_raw);
   __shared__ double s_lambda;
 
   const int tid = threadIdx.x;
-  const int rho = tid / T;
-  const int j = tid - rho * T;
+  const int rho = tid / (2 * T);
+  const int comp = (tid / T) & 1;
+  const int j = tid % T;
   const int y = blockIdx.x * ROWS + rho;
   const long long row_off = (long long)y * N;
 
-  C v[2][E];
+  C v[1][E];
+  const C* __restrict__ in = a.in[comp];
 #pragma unroll
-  for (int m = 0; m < E; ++m) {
-    v[0][m] = a.in[0][row_off + j + m * T];
-    v[1][m] = a.in[1][row_off + j + m * T];
-  }
-  const LineSmem<C, E> smv{sm + rho * LS, ROWS * LS};
+  for (int m = 0; m < E; ++m) v[0][m] = in[row_off + j + m * T];
+  // line (comp, rho) at sm + (comp*ROWS + rho)*LS
+  const LineSmem<C, E> smv{sm + (comp * ROWS + rho) * LS, 0};
 
   if (a.mode == kRowStep) {
+    // inverse x transform, result left in shared memory (natural order)
+    fft_lines<N, E, +1, 1, false, true>(v, j, smv, a.tw);
+    // lambda (and the populations) from the partials of the column pass;
+    // warp 0 does this after its own part of the transform, so the other
+    // warps are not held up
     if (tid < 32) {
-      double su0 = 0.0, su1 = 0.0, sw = 0.0;
-      for (int i = tid; i < 2 * a.ntile; i += 32) {
-        const double u = a.part[2 * i], w = a.part[2 * i + 1];
-        sw += w;
-        if (i < a.ntile) su0 += u; else su1 += u;
-      }
-      sw = warp_sum(sw);
-      if (tid == 0) s_lambda = sqrt(a.norm_num / sw);
-      if (a.pops != nullptr && blockIdx.x == 0) {
-        su0 = warp_sum(su0);
-        su1 = warp_sum(su1);
-        if (tid == 0) {
+      double su0, su1, sw;
+      sum_partials(a.part, a.ntile, tid, &su0, &su1, &sw);
+      if (tid == 0) {
+        s_lambda = sqrt(a.norm_num / sw);
+        if (a.pops != nullptr && blockIdx.x == 0) {
           a.pops[0] = a.atom_num * su0 / (su0 + su1);
           a.pops[1] = a.atom_num * su1 / (su0 + su1);
         }
@@ -186,70 +325,40 @@ row_kernel(const RowArgs<R> a) {
     }
     __syncthreads();
     const R lam = R(s_lambda);
-#pragma unroll
-    for (int m = 0; m < E; ++m) {
-      v[0][m] = cscale(v[0][m], lam);
-      v[1][m] = cscale(v[1][m], lam);
-    }
-    fft_lines<N, E, +1, 2>(v, j, smv, a.tw);
-
-    const RealOp<R>& op = a.op;
-#pragma unroll
-    for (int m = 0; m < E; ++m) {
-      const int x = j + m * T;
-      C p0 = v[0][m], p1 = v[1][m];
-      const R n0 = cabs2(p0), n1 = cabs2(p1);
-      // interaction half step (tensor_propagator.py:247-250)
-      const R e0 = fmadd(a.g_uu, n0, a.g_ud * n1);
-      const R e1 = fmadd(a.g_dd, n1, a.g_ud * n0);
-      const C i0 = cexp_z(op.zr, op.zi, e0);
-      const C i1 = cexp_z(op.zr, op.zi, e1);
-      p0 = cmul(p0, i0);
-      p1 = cmul(p1, i1);
-      C cc, s01, s10;
-      if (a.coupling) {  // first coupling half step (:252-254)
-        cc = fld(op.cc, x, y);
-        const C s = fld(op.cs, x, y), e = fld(op.ce, x, y);
-        s01 = cmulc(s, e);
-        s10 = cmul(s, e);
-        const C q0 = cadd(cmul(cc, p0), cmul(s01, p1));
-        const C q1 = cadd(cmul(s10, p0), cmul(cc, p1));
-        p0 = q0;
-        p1 = q1;
+    // point-wise operators: the 2T threads of a row share its N points
+    {
+      const LineSmem<C, E> r0{sm + rho * LS, 0};
+      const LineSmem<C, E> r1{sm + (ROWS + rho) * LS, 0};
+      RowFields<R> rf;
+      rf.init(a.op, y);
+      const int jj = tid % (2 * T);
+#pragma unroll kOpsUnroll
+      for (int m = 0; m < E / 2; ++m) {
+        const int x = jj + m * 2 * T;
+        C p0 = cscale(r0.ld(0, x), lam), p1 = cscale(r1.ld(0, x), lam);
+        real_space_ops<R>(p0, p1, x, rf, a);
+        r0.st(0, x, p0);
+        r1.st(0, x, p1);
       }
-      // potential full step (:256)
-      p0 = cmul(p0, cmul(fld(op.pa[0], x, y), fld(op.pb[0], x, y)));
-      p1 = cmul(p1, cmul(fld(op.pa[1], x, y), fld(op.pb[1], x, y)));
-      if (a.coupling) {  // second coupling half step (:258-260)
-        const C q0 = cadd(cmul(cc, p0), cmul(s01, p1));
-        const C q1 = cadd(cmul(s10, p0), cmul(cc, p1));
-        p0 = q0;
-        p1 = q1;
-      }
-      // second interaction half step with the same operator (:262-267)
-      v[0][m] = cmul(p0, i0);
-      v[1][m] = cmul(p1, i1);
     }
-    fft_lines<N, E, -1, 2>(v, j, smv, a.tw);
+    __syncthreads();
+    // forward x transform straight from shared memory
+    fft_lines<N, E, -1, 1, true, false>(v, j, smv, a.tw);
   } else {
-    if (a.mode == kRowForward) fft_lines<N, E, -1, 2>(v, j, smv, a.tw);
-    else fft_lines<N, E, +1, 2>(v, j, smv, a.tw);
+    if (a.mode == kRowForward) fft_lines<N, E, -1, 1>(v, j, smv, a.tw);
+    else fft_lines<N, E, +1, 1>(v, j, smv, a.tw);
 #pragma unroll
-    for (int m = 0; m < E; ++m) {
-      v[0][m] = cscale(v[0][m], a.scale);
-      v[1][m] = cscale(v[1][m], a.scale);
-    }
+    for (int m = 0; m < E; ++m) v[0][m] = cscale(v[0][m], a.scale);
   }
+  C* out = a.out[comp];
 #pragma unroll
-  for (int m = 0; m < E; ++m) {
-    a.out[0][row_off + j + m * T] = v[0][m];
-    a.out[1][row_off + j + m * T] = v[1][m];
-  }
+  for (int m = 0; m < E; ++m) out[row_off + j + m * T] = v[0][m];
+  (void)NT;
 }
 
 // -------------------------------------------------------------- column pass
-template <typename R, int N, int E, int COLS>
-__global__ void __launch_bounds__((N / E) * COLS)
+template <typename R, int N, int E, int COLS, int MINB>
+__global__ void __launch_bounds__((N / E) * COLS, MINB)
 col_kernel(const ColArgs<R> a) {
   using C = Cx<R>;
   constexpr int T = N / E;
@@ -257,7 +366,8 @@ col_kernel(const ColArgs<R> a) {
   constexpr int NT = T * COLS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* sm = reinterpret_cast<C*>(smem_raw);
-  __shared__ double s_red[2][NT / 32 > 0 ? NT / 32 : 1];
+  constexpr int NW = NT / 32;
+  __shared__ R s_red[2][NW];
 
   const int tid = threadIdx.x;
   const int c = tid % COLS;
@@ -280,27 +390,14 @@ col_kernel(const ColArgs<R> a) {
   const LineSmem<C, E> smv{sm + c * LS, 0};
   if (a.fwd) fft_lines<N, E, -1, 1>(v, j, smv, a.tw);
 
-  double su = 0.0, sw = 0.0;
-  if (a.has_kprev) {
-    const Field<R>& ka = a.kprev.a[comp];
-    const Field<R>& kb = a.kprev.b[comp];
-#pragma unroll
-    for (int m = 0; m < E; ++m) {
-      const int ky = j + m * T;
-      v[0][m] = cmul(v[0][m], cmul(fld(ka, x, ky), fld(kb, x, ky)));
-    }
-  }
+  R su = R(0), sw = R(0);
+  if (a.nk >= 1) apply_kinetic<R, E, T>(v[0], a.k1, comp, x, j);
   if (a.part != nullptr) su = thread_norm2(v[0]);
-  if (a.has_knext) {
-    const Field<R>& ka = a.knext.a[comp];
-    const Field<R>& kb = a.knext.b[comp];
-#pragma unroll
-    for (int m = 0; m < E; ++m) {
-      const int ky = j + m * T;
-      v[0][m] = cmul(v[0][m], cmul(fld(ka, x, ky), fld(kb, x, ky)));
-    }
+  sw = su;
+  if (a.nk >= 2) {
+    apply_kinetic<R, E, T>(v[0], a.k2, comp, x, j);
+    if (a.part != nullptr) sw = thread_norm2(v[0]);
   }
-  if (a.part != nullptr) sw = thread_norm2(v[0]);
   if (a.inv) fft_lines<N, E, +1, 1>(v, j, smv, a.tw);
   if (a.scale != R(1)) {
 #pragma unroll
@@ -320,15 +417,16 @@ col_kernel(const ColArgs<R> a) {
       s_red[1][warp] = sw;
     }
     __syncthreads();
-    if (tid == 0) {
-      double tu = 0.0, tw = 0.0;
-      for (int w = 0; w < NT / 32; ++w) {
-        tu += s_red[0][w];
-        tw += s_red[1][w];
+    if (warp == 0) {
+      R bu = lane < NW ? s_red[0][lane] : R(0);
+      R bw = lane < NW ? s_red[1][lane] : R(0);
+      bu = warp_sum(bu);
+      bw = warp_sum(bw);
+      if (lane == 0) {
+        double* dst = a.part + 2 * ((long long)comp * gridDim.x + blockIdx.x);
+        dst[0] = double(bu);
+        dst[1] = double(bw);
       }
-      double* dst = a.part + 2 * ((long long)comp * gridDim.x + blockIdx.x);
-      dst[0] = tu;
-      dst[1] = tw;
     }
   }
 }
@@ -338,15 +436,10 @@ col_kernel(const ColArgs<R> a) {
 // (tensor_tools.py:466-484).
 template <typename R>
 __global__ void __launch_bounds__(256) scale_kernel(const ScaleArgs<R> a) {
-  using C = Cx<R>;
   __shared__ double s_alpha;
   if (threadIdx.x < 32) {
-    double s0 = 0.0, s1 = 0.0;
-    for (int i = threadIdx.x; i < 2 * a.ntile; i += 32) {
-      if (i < a.ntile) s0 += a.part[2 * i]; else s1 += a.part[2 * i];
-    }
-    s0 = warp_sum(s0);
-    s1 = warp_sum(s1);
+    double s0, s1, sw;
+    sum_partials(a.part, a.ntile, threadIdx.x, &s0, &s1, &sw);
     if (threadIdx.x == 0) {
       s_alpha = sqrt(a.atom_num / (a.dv * (s0 + s1)));
       if (a.pops != nullptr && blockIdx.x == 0) {

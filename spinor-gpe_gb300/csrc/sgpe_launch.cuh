@@ -9,33 +9,58 @@ namespace sgpe {
 
 // Points per thread E and the preferred column-tile width per precision.
 // complex64: E = 16, 8 columns (64-byte row segments per column tile);
-// complex128: E = 8, 4 columns (also 64-byte segments).
+// complex128: E = 8, 4 columns (also 64-byte segments).  The complex64
+// values can be overridden at compile time (-DSGPE_F32_...) for tuning sweeps.
 template <typename R> struct Tune;
+// ROW_MINB / COL_MINB: resident blocks per SM requested from the compiler
+// (register cap); 2 makes every block of a 1024^2 pass co-resident.
+#ifndef SGPE_F32_ROW_E
+#define SGPE_F32_ROW_E 16
+#endif
+#ifndef SGPE_F32_ROW_THREADS
+#define SGPE_F32_ROW_THREADS 128
+#endif
+#ifndef SGPE_F32_ROW_MINB
+#define SGPE_F32_ROW_MINB 8
+#endif
+#ifndef SGPE_F32_COL_E
+#define SGPE_F32_COL_E 16
+#endif
+#ifndef SGPE_F32_COLS
+#define SGPE_F32_COLS 8
+#endif
+#ifndef SGPE_F32_COL_MINB
+#define SGPE_F32_COL_MINB 2
+#endif
 template <> struct Tune<float> {
-  static constexpr int E = 16, COLS = 8, ROW_THREADS = 256;
+  static constexpr int ROW_E = SGPE_F32_ROW_E, ROW_THREADS = SGPE_F32_ROW_THREADS, ROW_MINB = SGPE_F32_ROW_MINB;
+  static constexpr int COL_E = SGPE_F32_COL_E, COLS = SGPE_F32_COLS, COL_MINB = SGPE_F32_COL_MINB;
 };
 template <> struct Tune<double> {
-  static constexpr int E = 8, COLS = 4, ROW_THREADS = 256;
+  static constexpr int ROW_E = 8, ROW_THREADS = 256, ROW_MINB = 2;
+  static constexpr int COL_E = 8, COLS = 4, COL_MINB = 1;
 };
 
 constexpr int cmin(int a, int b) { return a < b ? a : b; }
 constexpr int cmax(int a, int b) { return a > b ? a : b; }
 
 template <typename R, int N> struct RowCfg {
-  static constexpr int E = cmin(N, Tune<R>::E);
+  static constexpr int E = cmin(N, Tune<R>::ROW_E);
   static constexpr int T = N / E;
-  // at least one warp per block, at most 16 rows
-  static constexpr int ROWS = cmax(cmax(cmin(Tune<R>::ROW_THREADS / T, 16), 1), 32 / T);
-  static constexpr int THREADS = T * ROWS;
+  // threads: 2 components x T per row; at least one warp, at most 16 rows
+  static constexpr int ROWS = cmax(cmax(cmin(Tune<R>::ROW_THREADS / (2 * T), 16), 1), 32 / (2 * T));
+  static constexpr int THREADS = 2 * T * ROWS;
   static constexpr size_t SMEM = 2ull * ROWS * (N + N / E) * sizeof(Cx<R>);
+  static constexpr int MINB = cmax(1, cmin(Tune<R>::ROW_MINB, 1024 / THREADS));
 };
 
 template <typename R, int N> struct ColCfg {
-  static constexpr int E = cmin(N, Tune<R>::E);
+  static constexpr int E = cmin(N, Tune<R>::COL_E);
   static constexpr int T = N / E;
   static constexpr int COLS = cmax(cmin(Tune<R>::COLS, 1024 / T), 32 / T);
   static constexpr int THREADS = T * COLS;
   static constexpr size_t SMEM = size_t(COLS) * (N + N / E + 2) * sizeof(Cx<R>);
+  static constexpr int MINB = cmax(1, cmin(Tune<R>::COL_MINB, 1024 / THREADS));
 };
 
 inline bool size_supported(int n) {
@@ -57,6 +82,19 @@ template <class F> inline cudaError_t dispatch_n(int n, F&& f) {
   }
 }
 
+// Raise a kernel's dynamic shared-memory limit once per device (the first
+// launch on that device); later launches skip the driver call.
+template <class K> inline cudaError_t smem_limit_once(K kernel, size_t bytes, unsigned long long* done_mask) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (*done_mask & bit) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+  if (e == cudaSuccess) *done_mask |= bit;
+  return e;
+}
+
 template <typename R> struct RowLauncher {
   const RowArgs<R>* a;
   int ny;
@@ -64,8 +102,9 @@ template <typename R> struct RowLauncher {
   template <int N> cudaError_t run() const {
     using Cfg = RowCfg<R, N>;
     if (ny % Cfg::ROWS != 0) return cudaErrorInvalidValue;
-    auto k = row_kernel<R, N, Cfg::E, Cfg::ROWS>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Cfg::SMEM));
+    auto k = row_kernel<R, N, Cfg::E, Cfg::ROWS, Cfg::MINB>;
+    static unsigned long long done = 0;
+    cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
     if (e != cudaSuccess) return e;
     k<<<ny / Cfg::ROWS, Cfg::THREADS, Cfg::SMEM, s>>>(*a);
     return cudaGetLastError();
@@ -80,8 +119,9 @@ template <typename R> struct ColLauncher {
     using Cfg = ColCfg<R, N>;
     const int nx = a->nx;
     if (nx % Cfg::COLS != 0 || (nx / 2) % Cfg::COLS != 0) return cudaErrorInvalidValue;
-    auto k = col_kernel<R, N, Cfg::E, Cfg::COLS>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Cfg::SMEM));
+    auto k = col_kernel<R, N, Cfg::E, Cfg::COLS, Cfg::MINB>;
+    static unsigned long long done = 0;
+    cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
     if (e != cudaSuccess) return e;
     k<<<dim3(nx / Cfg::COLS, 2), Cfg::THREADS, Cfg::SMEM, s>>>(*a);
     return cudaGetLastError();
@@ -102,6 +142,32 @@ template <typename R> cudaError_t launch_row(const RowArgs<R>& a, int nx, int ny
 
 template <typename R> cudaError_t launch_col(const ColArgs<R>& a, int ny, cudaStream_t s) {
   return dispatch_n(ny, ColLauncher<R>{&a, ny, s});
+}
+
+template <typename R> struct RowEQuery {
+  int* out;
+  template <int N> cudaError_t run() const {
+    *out = RowCfg<R, N>::E;
+    return cudaSuccess;
+  }
+};
+template <typename R> struct ColEQuery {
+  int* out;
+  template <int N> cudaError_t run() const {
+    *out = ColCfg<R, N>::E;
+    return cudaSuccess;
+  }
+};
+// Points per thread of the row (x) and column (y) transforms (0 if unsupported).
+template <typename R> int row_points_per_thread(int nx) {
+  int e = 0;
+  if (dispatch_n(nx, RowEQuery<R>{&e}) != cudaSuccess) return 0;
+  return e;
+}
+template <typename R> int col_points_per_thread(int ny) {
+  int e = 0;
+  if (dispatch_n(ny, ColEQuery<R>{&e}) != cudaSuccess) return 0;
+  return e;
 }
 
 // Column-tile width used for a column length ny (0 if unsupported).

@@ -10,8 +10,10 @@ import os
 
 import numpy as np
 
-LIB_PATH = os.path.join(os.path.dirname(os.path.dirname(
-    os.path.abspath(__file__))), 'libspinor_gb300.so')
+# SGPE_LIB_PATH selects another build of the same library (tuning builds).
+LIB_PATH = os.environ.get('SGPE_LIB_PATH') or os.path.join(
+    os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+    'libspinor_gb300.so')
 
 SGPE_OK = 0
 SGPE_ERR_ARG = 1

@@ -248,3 +248,55 @@ def test_large_and_extreme_shapes_conserve_norm(tp, tmp_path, shape):
     np.testing.assert_allclose(pops.cpu().numpy().sum(axis=1), 1.0,
                                atol=1e-9)
     assert abs(sum(calc_pops(psik, float(ps.space['dv_k']))) - 1.0) < 1e-5
+
+
+@pytest.mark.parametrize('dtype', [64, 128])
+def test_graph_replay_matches_eager_steps(tp, tmp_path, dtype, monkeypatch):
+    """Steady-state steps replayed from the plan's CUDA graphs give exactly
+    the state that eager launches of the same kernels give, and both match
+    the oracle."""
+    case = CASES['imag_raman_64']
+    p = case_params(case)
+    spin = spin_from_case(case, tmp_path)
+    a = tp.TensorPropagator(spin, p['dt'], 20, 'cuda', time=p['time'],
+                            dtype=dtype)
+    monkeypatch.setenv('SGPE_DISABLE_GRAPHS', '1')
+    b = tp.TensorPropagator(spin, p['dt'], 20, 'cuda', time=p['time'],
+                            dtype=dtype)
+    monkeypatch.delenv('SGPE_DISABLE_GRAPHS')
+    a.full_steps(20)                 # eager first step, then graphs (8, 8, 1, 1, 1)
+    b.full_steps(20)                 # eager throughout
+    for _ in range(3):
+        a.full_step()                # 1-step graph
+        b.full_step()
+    ga = np.array([t.cpu().numpy() for t in a.psik])
+    gb = np.array([t.cpu().numpy() for t in b.psik])
+    np.testing.assert_array_equal(ga, gb)
+    ref, _ = _oracle_run(inputs_from_arrays_case(case), p['dt'], p['time'], 23)
+    assert rel_l2(ga, ref) <= TOL[dtype]
+
+
+def inputs_from_arrays_case(case):
+    from oracle import inputs_from_arrays
+    return inputs_from_arrays(case)
+
+
+@pytest.mark.parametrize('name', ['imag_raman_64x32', 'imag_raman_64',
+                                  'real_raman_32', 'real_rot_32x64',
+                                  'imag_gradients_32', 'real_bump_32'])
+def test_complex64_error_not_worse_than_reference_complex64(tp, tmp_path, name):
+    """Over 40 steps, the complex64 drop-in stays as close to the complex128
+    reference as the original's own complex64 arithmetic does (up to 1.5x,
+    or 1e-5, whichever is larger)."""
+    case = CASES[name]
+    p = case_params(case)
+    n = 40
+    from oracle import inputs_from_arrays
+    ref128, _ = _oracle_run(inputs_from_arrays(case), p['dt'], p['time'], n, 128)
+    ref64, _ = _oracle_run(inputs_from_arrays(case), p['dt'], p['time'], n, 64)
+    bar = max(1e-5, 1.5 * rel_l2(ref64, ref128))
+    prop = tp.TensorPropagator(spin_from_case(case, tmp_path), p['dt'], n,
+                               'cuda', time=p['time'], dtype=64)
+    prop.full_steps(n)
+    got = np.array([t.cpu().numpy() for t in prop.psik])
+    assert rel_l2(got, ref128) <= bar

@@ -141,6 +141,30 @@ int sgpe_fft2(sgpe_plan* plan, const void* in0, const void* in1, void* out0, voi
  * Instrumentation of the native path; no counterpart in the original. */
 int sgpe_time_passes(sgpe_plan* plan, int n_steps, double* col_ms, double* row_ms, void* stream);
 
+/* Size in bytes of the device scratch array used by sgpe_fft2_static
+ * (2.25 MiB, present on every GPU that loads the library). */
+#define SGPE_FFT2_STATIC_BYTES (2359296)
+
+/* Allocation-free variant of sgpe_fft2, without a plan.  No counterpart in
+ * the original package.
+ * For callers that must not allocate device memory where they need the
+ * transform: code inside an open CUDA stream capture, hosts whose device
+ * memory belongs to their own pool allocator, real-time loops that cannot
+ * take an allocation's latency or implicit synchronisation, foreign-language
+ * hosts holding only raw device pointers.  It calls no cudaMalloc/cudaFree
+ * and no allocating library routine; the caller passes inputs and outputs.
+ * Scratch: a file-scope device array of SGPE_FFT2_STATIC_BYTES, enough for
+ * grids of up to 65,536 points in complex128 and 131,072 in complex64
+ * (e.g. 256x256 and 256x512); larger grids return SGPE_ERR_ARG with a
+ * message -- use sgpe_fft2 with a plan for those.
+ * Runs on the current CUDA device.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) and should be made before
+ * any stream capture on that device is started.  All calls share the array:
+ * calls that overlap on the GPU (other streams or threads) race -- order
+ * them on one stream.  Arguments and results as sgpe_fft2. */
+int sgpe_fft2_static(int ny, int nx, int dtype_bits, const void* in0, const void* in1, void* out0, void* out1,
+                     int inverse, double scale, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

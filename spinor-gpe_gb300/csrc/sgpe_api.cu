@@ -85,6 +85,11 @@ struct DeviceGuard {
 
 }  // namespace
 
+namespace sgpe_detail {
+// Sets this thread's sgpe_last_error message (used by other translation units).
+int set_error(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace sgpe_detail
+
 struct sgpe_plan {
   int ny = 0, nx = 0, bits = 0, device = 0;
   size_t elem = 0;           // bytes per complex element

@@ -1,0 +1,178 @@
+// Allocation-free centred 2-D transform (sgpe_fft2_static).
+//
+// Who needs it: callers that cannot call cudaMalloc (or anything that
+// allocates device memory) at the point where they want a transform --
+// code running while a CUDA stream capture is open, hosts whose device
+// memory is owned by their own pool allocator and must not be bypassed,
+// real-time loops that cannot afford an allocation's latency or implicit
+// synchronisation, and foreign-language hosts that hold only raw device
+// pointers.  sgpe_fft2 needs a plan, and creating a plan allocates; this
+// entry point needs nothing but the caller's input and output buffers.
+//
+// Its scratch (the field between the x and y passes and the per-stage
+// twiddle tables) is the file-scope array below, SGPE_FFT2_STATIC_BYTES
+// (2.25 MiB) on every GPU that loads the library, held until the process
+// exits.  Host code cannot use the array's name as a device address (it is a
+// host-side stand-in); the device address is looked up once per device with
+// cudaGetSymbolAddress, with that device current, on the first call made on
+// it.  That first call on a device should therefore come before any stream
+// capture is started on it.
+//
+// All calls share the one array and leave their data in it.  Nothing in it
+// has to start at zero: each call writes its twiddle tables and every
+// element of the intermediate field before reading them.  Calls whose work
+// overlaps on the GPU (different streams, or different host threads) race on
+// the array; order them on one stream.
+#include <cmath>
+#include <string>
+
+#include "sgpe_launch.cuh"
+#include "spinor_gb300.h"
+
+namespace sgpe_detail {
+int set_error(int code, const std::string& msg);  // sgpe_api.cu
+}
+
+namespace {
+
+static __device__ __align__(256) unsigned char g_fft2_scratch[SGPE_FFT2_STATIC_BYTES];
+
+constexpr int kMaxDevices = 64;
+void* g_scratch_dev[kMaxDevices] = {nullptr};
+
+// Device address of the scratch array on the current device (set-up on the
+// first call per device).
+int scratch_address(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return sgpe_detail::set_error(SGPE_ERR_CUDA, std::string("fft2_static: ") + cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices) return sgpe_detail::set_error(SGPE_ERR_ARG, "fft2_static: device index too large");
+  if (g_scratch_dev[dev] == nullptr) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_fft2_scratch);
+    if (e != cudaSuccess)
+      return sgpe_detail::set_error(SGPE_ERR_CUDA, std::string("fft2_static: cudaGetSymbolAddress: ") +
+                                                       cudaGetErrorString(e));
+    g_scratch_dev[dev] = p;
+  }
+  *out = g_scratch_dev[dev];
+  return SGPE_OK;
+}
+
+// Per-stage twiddle table of an (n, e) transform in the order the FFT engine
+// reads it (sgpe_fft.cuh): stage (ns, r_s) holds exp(-2 pi i k r/(ns r_s)) at
+// (r - 1) ns + k.  FP64 sincospi of the exactly reduced fraction, rounded once.
+template <typename R>
+__global__ void twiddle_kernel(sgpe::Cx<R>* out, int n, int e, int total) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  int off = 0, ns = 1;
+  while (ns < n) {
+    const int rs = (n / ns < e) ? n / ns : e;
+    const int cnt = (rs - 1) * ns;
+    if (i < off + cnt) {
+      const int r = (i - off) / ns + 1, k = (i - off) % ns;
+      const long long len = (long long)ns * rs;
+      const long long m = ((long long)k * r) % len;
+      double sn, cs;
+      sincospi(2.0 * double(m) / double(len), &sn, &cs);
+      out[i].x = R(cs);
+      out[i].y = R(-sn);
+      return;
+    }
+    off += cnt;
+    ns *= rs;
+  }
+}
+
+size_t round_up(size_t b) { return (b + 255) & ~size_t(255); }
+
+template <typename R>
+int run(int ny, int nx, const void* i0, const void* i1, void* o0, void* o1, int inverse, double scale,
+        cudaStream_t s) {
+  using C = sgpe::Cx<R>;
+  const int ex = sgpe::row_points_per_thread<R>(nx), ey = sgpe::col_points_per_thread<R>(ny);
+  const int cols = sgpe::col_tile_width<R>(ny);
+  if (ex == 0 || ey == 0 || cols == 0 || nx % cols != 0 || (nx / 2) % cols != 0)
+    return sgpe_detail::set_error(SGPE_ERR_ARG, "fft2_static: unsupported grid size");
+  const int twx = sgpe::tw_offset(nx, ex, nx), twy = sgpe::tw_offset(ny, ey, ny);
+  const size_t field = round_up(sizeof(C) * (size_t)nx * ny);
+  const size_t need = 2 * field + round_up(sizeof(C) * (twx > 0 ? twx : 1)) + round_up(sizeof(C) * (twy > 0 ? twy : 1));
+  if (need > size_t(SGPE_FFT2_STATIC_BYTES))
+    return sgpe_detail::set_error(
+        SGPE_ERR_ARG, "fft2_static: a " + std::to_string(ny) + "x" + std::to_string(nx) + " complex" +
+                          std::to_string(8 * sizeof(C)) + " transform needs " + std::to_string(need) +
+                          " bytes of scratch; the static scratch holds " + std::to_string(SGPE_FFT2_STATIC_BYTES) +
+                          " (use sgpe_fft2 with a plan for larger grids)");
+  void* base = nullptr;
+  int rc = scratch_address(&base);
+  if (rc != SGPE_OK) return rc;
+  unsigned char* b = static_cast<unsigned char*>(base);
+  C* mid0 = reinterpret_cast<C*>(b);
+  C* mid1 = reinterpret_cast<C*>(b + field);
+  C* tw_x = reinterpret_cast<C*>(b + 2 * field);
+  C* tw_y = reinterpret_cast<C*>(b + 2 * field + round_up(sizeof(C) * (twx > 0 ? twx : 1)));
+  if (twx > 0) twiddle_kernel<R><<<(twx + 255) / 256, 256, 0, s>>>(tw_x, nx, ex, twx);
+  if (twy > 0) twiddle_kernel<R><<<(twy + 255) / 256, 256, 0, s>>>(tw_y, ny, ey, twy);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return sgpe_detail::set_error(SGPE_ERR_CUDA, std::string("fft2_static: ") + cudaGetErrorString(e));
+
+  sgpe::RowArgs<R> r{};
+  r.tw = tw_x;
+  sgpe::ColArgs<R> c{};
+  c.tw = tw_y;
+  c.nx = nx;
+  c.scale = R(1);
+  if (!inverse) {  // x transform into the scratch, then y transform with centring
+    r.in[0] = static_cast<const C*>(i0);
+    r.in[1] = static_cast<const C*>(i1);
+    r.out[0] = mid0;
+    r.out[1] = mid1;
+    r.mode = sgpe::kRowForward;
+    r.scale = R(1);
+    e = sgpe::launch_row<R>(r, nx, ny, s);
+    if (e == cudaSuccess) {
+      c.in[0] = mid0;
+      c.in[1] = mid1;
+      c.out[0] = static_cast<C*>(o0);
+      c.out[1] = static_cast<C*>(o1);
+      c.fwd = 1;
+      c.out_shift = 1;
+      c.scale = R(scale);
+      e = sgpe::launch_col<R>(c, ny, s);
+    }
+  } else {  // un-centring y transform into the scratch, then x transform
+    c.in[0] = static_cast<const C*>(i0);
+    c.in[1] = static_cast<const C*>(i1);
+    c.out[0] = mid0;
+    c.out[1] = mid1;
+    c.inv = 1;
+    c.in_shift = 1;
+    e = sgpe::launch_col<R>(c, ny, s);
+    if (e == cudaSuccess) {
+      r.in[0] = mid0;
+      r.in[1] = mid1;
+      r.out[0] = static_cast<C*>(o0);
+      r.out[1] = static_cast<C*>(o1);
+      r.mode = sgpe::kRowInverse;
+      r.scale = R(scale);
+      e = sgpe::launch_row<R>(r, nx, ny, s);
+    }
+  }
+  if (e != cudaSuccess) return sgpe_detail::set_error(SGPE_ERR_CUDA, std::string("fft2_static: ") + cudaGetErrorString(e));
+  return SGPE_OK;
+}
+
+}  // namespace
+
+extern "C" int sgpe_fft2_static(int ny, int nx, int dtype_bits, const void* in0, const void* in1, void* out0,
+                                void* out1, int inverse, double scale, void* stream) {
+  if (!in0 || !in1 || !out0 || !out1) return sgpe_detail::set_error(SGPE_ERR_ARG, "fft2_static: null data pointer");
+  if (!sgpe::size_supported(nx) || !sgpe::size_supported(ny))
+    return sgpe_detail::set_error(SGPE_ERR_ARG, "fft2_static: grid sizes must be powers of two in [32, 4096]");
+  if (dtype_bits != 64 && dtype_bits != 128)
+    return sgpe_detail::set_error(SGPE_ERR_ARG, "fft2_static: dtype_bits must be 64 or 128");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return dtype_bits == 64 ? run<float>(ny, nx, in0, in1, out0, out1, inverse, scale, s)
+                          : run<double>(ny, nx, in0, in1, out0, out1, inverse, scale, s);
+}

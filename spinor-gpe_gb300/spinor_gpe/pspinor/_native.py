@@ -24,7 +24,8 @@ SGPE_ERR_OOM = 4
 EXPORTED = ('sgpe_version', 'sgpe_last_error', 'sgpe_plan_create',
             'sgpe_plan_destroy', 'sgpe_set_physics', 'sgpe_set_substep',
             'sgpe_load_psik', 'sgpe_store_psik', 'sgpe_single_step',
-            'sgpe_full_steps', 'sgpe_fft2', 'sgpe_time_passes')
+            'sgpe_full_steps', 'sgpe_fft2', 'sgpe_time_passes',
+            'sgpe_fft2_static')
 
 
 class SgpeError(RuntimeError):
@@ -69,6 +70,9 @@ _SIGS = {
                    _VP], ctypes.c_int),
     'sgpe_time_passes': ([_VP, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                           ctypes.POINTER(ctypes.c_double), _VP], ctypes.c_int),
+    'sgpe_fft2_static': ([ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP,
+                          _VP, _VP, ctypes.c_int, ctypes.c_double, _VP],
+                         ctypes.c_int),
 }
 
 _LIB = None

@@ -34,6 +34,26 @@ namespace sgpe {
 
 constexpr int kOpsUnroll = SGPE_OPS_UNROLL;
 
+// Programmatic dependent launch: the pass kernels are launched so that they
+// may start while the previous kernel in the stream is finishing.  Before
+// reading anything the previous kernel wrote, a kernel waits for that grid to
+// complete (griddepcontrol.wait); once it has loaded its own inputs it lets
+// the next kernel be scheduled (griddepcontrol.launch_dependents), which only
+// moves that kernel's launch earlier -- its own wait still orders the data.
+#ifndef SGPE_PDL
+#define SGPE_PDL 1
+#endif
+__device__ __forceinline__ void wait_for_previous_grid() {
+#if SGPE_PDL
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
+__device__ __forceinline__ void allow_next_grid() {
+#if SGPE_PDL
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
+
 // A complex operator field with broadcast strides: value(x, y) = p[x*sx + y*sy].
 // sx = sy = 0 is a uniform value, (1, 0) an x-table, (0, 1) a y-table and
 // (1, Nx) a full field.
@@ -301,8 +321,10 @@ row_kernel(const RowArgs<R> a) {
 
   C v[1][E];
   const C* __restrict__ in = a.in[comp];
+  wait_for_previous_grid();
 #pragma unroll
   for (int m = 0; m < E; ++m) v[0][m] = in[row_off + j + m * T];
+  allow_next_grid();
   // line (comp, rho) at sm + (comp*ROWS + rho)*LS
   const LineSmem<C, E> smv{sm + (comp * ROWS + rho) * LS, 0};
 
@@ -382,11 +404,13 @@ col_kernel(const ColArgs<R> a) {
   C* out = a.out[comp];
 
   C v[1][E];
+  wait_for_previous_grid();
 #pragma unroll
   for (int m = 0; m < E; ++m) {
     const int row = j + (a.in_shift ? (m + E / 2) % E : m) * T;
     v[0][m] = in[(long long)row * nx + xin];
   }
+  allow_next_grid();
   const LineSmem<C, E> smv{sm + c * LS, 0};
   if (a.fwd) fft_lines<N, E, -1, 1>(v, j, smv, a.tw);
 

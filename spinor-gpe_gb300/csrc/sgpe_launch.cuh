@@ -95,6 +95,28 @@ template <class K> inline cudaError_t smem_limit_once(K kernel, size_t bytes, un
   return e;
 }
 
+// Launch with programmatic stream serialisation (see SGPE_PDL), so the
+// kernel may be scheduled while its predecessor drains.
+template <class K, class A>
+inline cudaError_t launch_pdl(K kernel, dim3 grid, dim3 block, size_t smem, cudaStream_t s, const A& args) {
+#if SGPE_PDL
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args);
+#else
+  kernel<<<grid, block, smem, s>>>(args);
+  return cudaGetLastError();
+#endif
+}
+
 template <typename R> struct RowLauncher {
   const RowArgs<R>* a;
   int ny;
@@ -106,8 +128,7 @@ template <typename R> struct RowLauncher {
     static unsigned long long done = 0;
     cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
     if (e != cudaSuccess) return e;
-    k<<<ny / Cfg::ROWS, Cfg::THREADS, Cfg::SMEM, s>>>(*a);
-    return cudaGetLastError();
+    return launch_pdl(k, dim3(ny / Cfg::ROWS), dim3(Cfg::THREADS), Cfg::SMEM, s, *a);
   }
 };
 
@@ -123,8 +144,7 @@ template <typename R> struct ColLauncher {
     static unsigned long long done = 0;
     cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
     if (e != cudaSuccess) return e;
-    k<<<dim3(nx / Cfg::COLS, 2), Cfg::THREADS, Cfg::SMEM, s>>>(*a);
-    return cudaGetLastError();
+    return launch_pdl(k, dim3(nx / Cfg::COLS, 2), dim3(Cfg::THREADS), Cfg::SMEM, s, *a);
   }
 };
 

@@ -45,7 +45,8 @@ struct HostField {
 };
 
 struct SubOps {
-  DevField kin_a[2], kin_b[2], pot_a[2], pot_b[2], cc, cs, ce;
+  DevField kin_a[2], kin_b[2], pot_a[2], pot_b[2], cc, cs, ce, s01, s10;
+  bool has_s01 = false;
   HostField kin_host[2][2];  // [comp][a, b]
   double zr = 0.0, zi = 0.0;
   std::vector<void*> allocs;
@@ -195,8 +196,17 @@ int upload_host_field(sgpe_plan* p, const HostField& hf, DevField* out, std::vec
   return rc;
 }
 
-// Element-wise product of two broadcast fields, evaluated in FP64.
-HostField multiply_fields(const HostField& fa, const HostField& fb, int nx, int ny) {
+HostField host_copy(const sgpe_field& f) {
+  HostField h;
+  h.v.assign(f.data, f.data + 2 * (size_t)f.n);
+  h.sx = f.sx;
+  h.sy = f.sy;
+  return h;
+}
+
+// Element-wise product of two broadcast fields, evaluated in FP64 (with
+// the second factor conjugated when conj_b).
+HostField multiply_fields(const HostField& fa, const HostField& fb, int nx, int ny, bool conj_b = false) {
   HostField r;
   if (fa.sx == fb.sx && fa.sy == fb.sy) {
     r.sx = fa.sx;
@@ -222,7 +232,7 @@ HostField multiply_fields(const HostField& fa, const HostField& fb, int nx, int 
       const long long ib = (long long)x * fb.sx + (long long)y * fb.sy;
       const long long ir = (long long)x * r.sx + (long long)y * r.sy;
       const double ar = fa.v[2 * ia], ai = fa.v[2 * ia + 1];
-      const double br = fb.v[2 * ib], bi = fb.v[2 * ib + 1];
+      const double br = fb.v[2 * ib], bi = conj_b ? -fb.v[2 * ib + 1] : fb.v[2 * ib + 1];
       r.v[2 * ir] = ar * br - ai * bi;
       r.v[2 * ir + 1] = ar * bi + ai * br;
     }
@@ -283,6 +293,9 @@ template <typename R> sgpe::RealOp<R> real_op(const SubOps& so) {
   o.cc = typed<R>(so.cc);
   o.cs = typed<R>(so.cs);
   o.ce = typed<R>(so.ce);
+  o.has_s01 = so.has_s01 ? 1 : 0;
+  o.s01 = typed<R>(so.has_s01 ? so.s01 : so.cs);
+  o.s10 = typed<R>(so.has_s01 ? so.s10 : so.cs);
   o.zr = R(so.zr);
   o.zi = R(so.zi);
   return o;
@@ -632,6 +645,20 @@ int sgpe_set_substep(sgpe_plan* p, int sub, const sgpe_substep_ops* ops) {
   if (rc == SGPE_OK) rc = upload_field(p, ops->cpl_c, &so.cc, &so, "cpl_c");
   if (rc == SGPE_OK) rc = upload_field(p, ops->cpl_s, &so.cs, &so, "cpl_s");
   if (rc == SGPE_OK) rc = upload_field(p, ops->cpl_e, &so.ce, &so, "cpl_e");
+  if (rc == SGPE_OK) {
+    // s conj(e) and s e in FP64, when the products stay compact (1-D or
+    // uniform) or the factors are full fields anyway
+    const HostField hs = host_copy(ops->cpl_s), he = host_copy(ops->cpl_e);
+    HostField m01 = multiply_fields(hs, he, p->nx, p->ny, true);
+    HostField m10 = multiply_fields(hs, he, p->nx, p->ny, false);
+    const bool product_full = (m01.sx == 1 && m01.sy == p->nx);
+    const bool factor_full = (hs.sx == 1 && hs.sy == p->nx) || (he.sx == 1 && he.sy == p->nx);
+    if (!product_full || factor_full) {
+      rc = upload_host_field(p, m01, &so.s01, &so.allocs);
+      if (rc == SGPE_OK) rc = upload_host_field(p, m10, &so.s10, &so.allocs);
+      so.has_s01 = (rc == SGPE_OK);
+    }
+  }
   if (rc != SGPE_OK) {
     free_sub(so);
     return rc;

@@ -27,7 +27,7 @@
 // Unroll factor of the row kernel's point-wise loop (small: keeps the code
 // within the instruction cache).
 #ifndef SGPE_OPS_UNROLL
-#define SGPE_OPS_UNROLL 2
+#define SGPE_OPS_UNROLL 4
 #endif
 
 namespace sgpe {
@@ -78,11 +78,15 @@ template <typename R> struct KinOp {
 template <typename R> struct RealOp {
   Field<R> pa[2], pb[2];
   Field<R> cc, cs, ce;
+  // off-diagonal coupling elements s conj(e) and s e, pre-multiplied in FP64
+  // on the host when that keeps them 1-D tables (has_s01), else computed here
+  Field<R> s01, s10;
+  int has_s01;
   R zr, zi;
 };
 
 // Field slots of RealOp in a fixed order (for the per-row hoisting below).
-enum { kPa0 = 0, kPb0, kPa1, kPb1, kCc, kCs, kCe, kNumRealFields };
+enum { kPa0 = 0, kPb0, kPa1, kPb1, kCc, kCs, kCe, kS01, kS10, kNumRealFields };
 
 template <typename R> __device__ __forceinline__ const Field<R>& real_field(const RealOp<R>& op, int k) {
   switch (k) {
@@ -92,21 +96,39 @@ template <typename R> __device__ __forceinline__ const Field<R>& real_field(cons
     case kPb1: return op.pb[1];
     case kCc: return op.cc;
     case kCs: return op.cs;
-    default: return op.ce;
+    case kCe: return op.ce;
+    case kS01: return op.s01;
+    default: return op.s10;
   }
 }
 
 // The real-space operator values along one row y.  Fields that do not vary
-// along x (uniform values, y-tables) resolve to one address per row, which a
-// warp reads as a single broadcast.
+// along x (uniform values, y-tables) are loaded once per row into registers
+// (the row pass runs its point-wise loop while the transform data sits in
+// shared memory, so registers are free then); the others are read per point.
 template <typename R> struct RowFields {
   const RealOp<R>* op;
   int y;
+  unsigned row_const;
+  Cx<R> h[kNumRealFields];
   __device__ __forceinline__ void init(const RealOp<R>& o, int yy) {
     op = &o;
     y = yy;
+    row_const = 0;
+#pragma unroll
+    for (int k = 0; k < kNumRealFields; ++k) {
+      const Field<R>& f = real_field(o, k);
+      if (f.sx == 0) {
+        row_const |= 1u << k;
+        h[k] = fld(f, 0, y);
+      } else {
+        h[k] = Cx<R>{};
+      }
+    }
   }
-  __device__ __forceinline__ Cx<R> at(int k, int x) const { return fld(real_field(*op, k), x, y); }
+  __device__ __forceinline__ Cx<R> at(int k, int x) const {
+    return ((row_const >> k) & 1u) ? h[k] : fld(real_field(*op, k), x, y);
+  }
 };
 
 enum RowMode { kRowStep = 0, kRowForward = 1, kRowInverse = 2 };
@@ -258,9 +280,14 @@ __device__ __forceinline__ void real_space_ops(Cx<R>& p0, Cx<R>& p1, int x, cons
   C cc, s01, s10;
   if (a.coupling) {
     cc = rf.at(kCc, x);
-    const C sv = rf.at(kCs, x), e = rf.at(kCe, x);
-    s01 = cmulc(sv, e);
-    s10 = cmul(sv, e);
+    if (op.has_s01) {
+      s01 = rf.at(kS01, x);
+      s10 = rf.at(kS10, x);
+    } else {
+      const C sv = rf.at(kCs, x), e = rf.at(kCe, x);
+      s01 = cmulc(sv, e);
+      s10 = cmul(sv, e);
+    }
     const C q0 = cadd(cmul(cc, p0), cmul(s01, p1));
     const C q1 = cadd(cmul(s10, p0), cmul(cc, p1));
     p0 = q0;

@@ -132,6 +132,38 @@ int sgpe_full_steps(sgpe_plan* plan, int n_steps, double* pops_dev, void* stream
 int sgpe_fft2(sgpe_plan* plan, const void* in0, const void* in1, void* out0, void* out1,
               int inverse, double scale, void* stream);
 
+/* Energy fields (FP64, real parts used; each energy is the sum of two
+ * broadcast fields a + b, so separable energies stay 1-D tables):
+ *  kin_a[c] + kin_b[c] = K_c(kx, ky) in centred k order (the order of psik),
+ *  pot_a[c] + pot_b[c] = V_c(x, y),
+ *  cpl = h(x, y), the coupling energy density being 2 Re(conj(psi_0) h psi_1);
+ *  h = (Omega/2) exp(-i theta) is the upper off-diagonal of the coupling
+ *  Hamiltonian the propagator applies. */
+typedef struct sgpe_energy_fields {
+  sgpe_field kin_a[2];
+  sgpe_field kin_b[2];
+  sgpe_field pot_a[2];
+  sgpe_field pot_b[2];
+  sgpe_field cpl;
+} sgpe_energy_fields;
+
+/* Store energy fields in slot 0 or 1 of the plan (e.g. the physical energy
+ * and the original package's reporting convention).  Synchronous. */
+int sgpe_set_energy_fields(sgpe_plan* plan, int slot, const sgpe_energy_fields* fields);
+
+/* FP64 energy of the spinor psik (device pointers, centred k order) with the
+ * fields of `slot`; writes 10 doubles to out_dev (device):
+ *   [E_kin, E_pot, E_int, E_cpl, E_total, mu, N_k, N_r, S1, S2]
+ * E_kin = sum_k K_c |psik_c|^2 dv_k (spectral), E_pot = sum V_c n_c dv_r,
+ * E_int = sum (g_uu n0^2/2 + g_dd n1^2/2 + g_ud n0 n1) dv_r,
+ * E_cpl = sum 2 Re(conj(psi_0) h psi_1) dv_r, mu = (E_kin + E_pot + E_cpl +
+ * 2 E_int) / N_r, N_k / N_r the atom numbers in k / real space,
+ * S1 = sum (g_uu n0^2 + g_dd n1^2) dv_r, S2 = sum g_ud n0 n1 dv_r, with
+ * psi = ifft_2d(psik).  Replaces the host-side energy expectation value
+ * (spinor_gpe/pspinor/tensor_propagator.py:273-324); the kinetic term is
+ * spectral instead of finite differences of the unwrapped phase. */
+int sgpe_energy(sgpe_plan* plan, int slot, const void* psik0, const void* psik1, double* out_dev, void* stream);
+
 /* Measurement helper: n_steps full steps exactly as sgpe_full_steps (no
  * populations), captured into a CUDA graph with events around every column
  * pass and every row pass, launched once on `stream`.  Synchronises the

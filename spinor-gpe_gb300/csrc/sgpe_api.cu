@@ -16,6 +16,7 @@
 #include <string>
 #include <vector>
 
+#include "sgpe_energy.cuh"
 #include "sgpe_launch.cuh"
 #include "spinor_gb300.h"
 
@@ -49,6 +50,13 @@ struct SubOps {
   bool has_s01 = false;
   HostField kin_host[2][2];  // [comp][a, b]
   double zr = 0.0, zi = 0.0;
+  std::vector<void*> allocs;
+  bool set = false;
+};
+
+// FP64 energy fields of one slot (sgpe_set_energy_fields).
+struct EnergyFields {
+  DevField kin_a[2], kin_b[2], pot_a[2], pot_b[2], cpl;
   std::vector<void*> allocs;
   bool set = false;
 };
@@ -102,6 +110,9 @@ struct sgpe_plan {
   void* tw_y = nullptr;
   SubOps sub[2];
   PairOps pair[2][2];        // [prev][next]
+  EnergyFields efield[2];
+  void* epsi[2] = {nullptr, nullptr};   // real-space spinor for the energy
+  double* epart = nullptr;              // energy block partials [2][kEnergyBlocks][6]
   double g[3] = {0, 0, 0};
   double atom_num = 1.0, dv_r = 1.0, dv_k = 1.0;
   int coupling = 0;
@@ -237,6 +248,35 @@ HostField multiply_fields(const HostField& fa, const HostField& fb, int nx, int 
       r.v[2 * ir + 1] = ar * bi + ai * br;
     }
   return r;
+}
+
+constexpr int kEnergyBlocks = 304;
+
+// FP64 upload of a field (energy fields keep double precision).
+int upload_field64(sgpe_plan* p, const sgpe_field& f, DevField* out, std::vector<void*>* allocs, const char* name) {
+  if (f.data == nullptr || f.n < 1 || f.sx < 0 || f.sy < 0)
+    return fail(SGPE_ERR_ARG, std::string("field ") + name + ": null data, empty or negative stride");
+  const long long last = (long long)(p->nx - 1) * f.sx + (long long)(p->ny - 1) * f.sy;
+  if (last >= f.n) return fail(SGPE_ERR_ARG, std::string("field ") + name + ": strides exceed its data");
+  void* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(double2) * f.n);
+  if (e != cudaSuccess) return fail(SGPE_ERR_OOM, std::string("field ") + name + ": " + cudaGetErrorString(e));
+  allocs->push_back(d);
+  e = cudaMemcpy(d, f.data, sizeof(double2) * f.n, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "energy field upload");
+  out->p = d;
+  out->sx = f.sx;
+  out->sy = f.sy;
+  return SGPE_OK;
+}
+
+void free_efield(EnergyFields& ef) {
+  for (void* q : ef.allocs) cudaFree(q);
+  ef = EnergyFields();
+}
+
+sgpe::Field<double> typed64(const DevField& f) {
+  return sgpe::Field<double>{static_cast<const double2*>(f.p), f.sx, f.sy};
 }
 
 void free_pair(PairOps& po) {
@@ -470,6 +510,58 @@ template <typename R> int fft2(sgpe_plan* p, const void* i0, const void* i1, voi
 
 bool ready(sgpe_plan* p) { return p->physics && p->sub[0].set && p->sub[1].set; }
 
+template <typename R>
+int energy_impl(sgpe_plan* p, int slot, const void* k0, const void* k1, double* out, cudaStream_t s) {
+  const EnergyFields& ef = p->efield[slot];
+  const long long n = (long long)p->nx * p->ny;
+  for (int c = 0; c < 2; ++c) {
+    if (p->epsi[c] == nullptr) {
+      cudaError_t e = cudaMalloc(&p->epsi[c], p->elem * n);
+      if (e != cudaSuccess) return fail(SGPE_ERR_OOM, std::string("energy buffer: ") + cudaGetErrorString(e));
+    }
+  }
+  if (p->epart == nullptr) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p->epart), sizeof(double) * 2 * kEnergyBlocks * sgpe::kEnergySums);
+    if (e != cudaSuccess) return fail(SGPE_ERR_OOM, std::string("energy partials: ") + cudaGetErrorString(e));
+  }
+  sgpe::EnergyArgs<R> a{};
+  a.n = n;
+  a.nx = p->nx;
+  a.g_uu = p->g[0];
+  a.g_dd = p->g[1];
+  a.g_ud = p->g[2];
+  a.h = typed64(ef.cpl);
+  // k-space pass on psik
+  a.a[0] = cst<R>(k0);
+  a.a[1] = cst<R>(k1);
+  for (int c = 0; c < 2; ++c) {
+    a.w[c] = typed64(ef.kin_a[c]);
+    a.wb[c] = typed64(ef.kin_b[c]);
+  }
+  a.part = p->epart;
+  sgpe::energy_k_kernel<R><<<kEnergyBlocks, 256, 0, s>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "energy (k pass)");
+  // psi = ifft_2d(psik): unnormalised inverse over N points, times 2 pi/(dx dy)
+  const double dxdy = p->dv_r;
+  const int rc = fft2<R>(p, k0, k1, p->epsi[0], p->epsi[1], 1, 6.283185307179586476925286766559 / (double(n) * dxdy), s);
+  if (rc != SGPE_OK) return rc;
+  a.a[0] = cst<R>(p->epsi[0]);
+  a.a[1] = cst<R>(p->epsi[1]);
+  for (int c = 0; c < 2; ++c) {
+    a.w[c] = typed64(ef.pot_a[c]);
+    a.wb[c] = typed64(ef.pot_b[c]);
+  }
+  a.part = p->epart + kEnergyBlocks * sgpe::kEnergySums;
+  sgpe::energy_r_kernel<R><<<kEnergyBlocks, 256, 0, s>>>(a);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "energy (real-space pass)");
+  sgpe::energy_finalize_kernel<<<1, 32, 0, s>>>(p->epart, p->epart + kEnergyBlocks * sgpe::kEnergySums,
+                                                kEnergyBlocks, p->dv_k, p->dv_r, out);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? SGPE_OK : cuda_fail(e, "energy (finalise)");
+}
+
 void drop_graphs(sgpe_plan* p) {
   for (auto& g : p->graph) {
     if (g) cudaGraphExecDestroy(g);
@@ -608,6 +700,11 @@ int sgpe_plan_destroy(sgpe_plan* p) {
   free_sub(p->sub[1]);
   for (int i = 0; i < 2; ++i)
     for (int k = 0; k < 2; ++k) free_pair(p->pair[i][k]);
+  free_efield(p->efield[0]);
+  free_efield(p->efield[1]);
+  for (int c = 0; c < 2; ++c)
+    if (p->epsi[c]) cudaFree(p->epsi[c]);
+  if (p->epart) cudaFree(p->epart);
   delete p;
   return SGPE_OK;
 }
@@ -748,6 +845,40 @@ int sgpe_full_steps(sgpe_plan* p, int n_steps, double* pops, void* stream) {
   if (rc != SGPE_OK) return rc;
   if (pops != nullptr && n_steps > 0) p->pending_pops = pops + 2 * (n_steps - 1);
   return SGPE_OK;
+}
+
+int sgpe_set_energy_fields(sgpe_plan* p, int slot, const sgpe_energy_fields* f) {
+  if (p == nullptr || f == nullptr) return fail(SGPE_ERR_ARG, "null plan or fields");
+  if (slot != 0 && slot != 1) return fail(SGPE_ERR_ARG, "slot must be 0 or 1");
+  DeviceGuard g(p->device);
+  EnergyFields ef;
+  int rc = SGPE_OK;
+  for (int c = 0; c < 2 && rc == SGPE_OK; ++c) {
+    rc = upload_field64(p, f->kin_a[c], &ef.kin_a[c], &ef.allocs, "energy kin_a");
+    if (rc == SGPE_OK) rc = upload_field64(p, f->kin_b[c], &ef.kin_b[c], &ef.allocs, "energy kin_b");
+    if (rc == SGPE_OK) rc = upload_field64(p, f->pot_a[c], &ef.pot_a[c], &ef.allocs, "energy pot_a");
+    if (rc == SGPE_OK) rc = upload_field64(p, f->pot_b[c], &ef.pot_b[c], &ef.allocs, "energy pot_b");
+  }
+  if (rc == SGPE_OK) rc = upload_field64(p, f->cpl, &ef.cpl, &ef.allocs, "energy cpl");
+  if (rc != SGPE_OK) {
+    free_efield(ef);
+    return rc;
+  }
+  ef.set = true;
+  free_efield(p->efield[slot]);
+  p->efield[slot] = std::move(ef);
+  return SGPE_OK;
+}
+
+int sgpe_energy(sgpe_plan* p, int slot, const void* k0, const void* k1, double* out, void* stream) {
+  if (p == nullptr || k0 == nullptr || k1 == nullptr || out == nullptr)
+    return fail(SGPE_ERR_ARG, "null plan, psik or output pointer");
+  if (slot != 0 && slot != 1) return fail(SGPE_ERR_ARG, "slot must be 0 or 1");
+  if (!p->efield[slot].set) return fail(SGPE_ERR_STATE, "energy fields of this slot not set");
+  if (!p->physics) return fail(SGPE_ERR_STATE, "physics not set");
+  DeviceGuard g(p->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return p->bits == 64 ? energy_impl<float>(p, slot, k0, k1, out, s) : energy_impl<double>(p, slot, k0, k1, out, s);
 }
 
 int sgpe_time_passes(sgpe_plan* p, int n_steps, double* col_ms, double* row_ms, void* stream) {

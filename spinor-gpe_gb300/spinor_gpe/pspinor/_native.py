@@ -25,7 +25,7 @@ EXPORTED = ('sgpe_version', 'sgpe_last_error', 'sgpe_plan_create',
             'sgpe_plan_destroy', 'sgpe_set_physics', 'sgpe_set_substep',
             'sgpe_load_psik', 'sgpe_store_psik', 'sgpe_single_step',
             'sgpe_full_steps', 'sgpe_fft2', 'sgpe_time_passes',
-            'sgpe_fft2_static')
+            'sgpe_fft2_static', 'sgpe_set_energy_fields', 'sgpe_energy')
 
 
 class SgpeError(RuntimeError):
@@ -51,6 +51,12 @@ class SubstepOps(ctypes.Structure):
                 ('int_z_re', ctypes.c_double), ('int_z_im', ctypes.c_double)]
 
 
+class EnergyFields(ctypes.Structure):
+    """``sgpe_energy_fields``."""
+    _fields_ = [('kin_a', Field * 2), ('kin_b', Field * 2),
+                ('pot_a', Field * 2), ('pot_b', Field * 2), ('cpl', Field)]
+
+
 _VP = ctypes.c_void_p
 _SIGS = {
     'sgpe_version': ([], ctypes.c_int),
@@ -70,6 +76,9 @@ _SIGS = {
                    _VP], ctypes.c_int),
     'sgpe_time_passes': ([_VP, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                           ctypes.POINTER(ctypes.c_double), _VP], ctypes.c_int),
+    'sgpe_set_energy_fields': ([_VP, ctypes.c_int, ctypes.POINTER(EnergyFields)],
+                               ctypes.c_int),
+    'sgpe_energy': ([_VP, ctypes.c_int, _VP, _VP, _VP, _VP], ctypes.c_int),
     'sgpe_fft2_static': ([ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP,
                           _VP, _VP, ctypes.c_int, ctypes.c_double, _VP],
                          ctypes.c_int),
@@ -196,6 +205,31 @@ class Plan:
                                       ctypes.byref(row),
                                       _stream(torch, device)))
         return col.value, row.value
+
+    def set_energy_fields(self, slot, kin, pot, cpl):
+        """Upload FP64 energy fields: ``kin`` and ``pot`` are two (a, b)
+        FieldSpec pairs per component (the energy is a + b), ``cpl`` the
+        coupling field h."""
+        ef = EnergyFields()
+        keep = []
+
+        def put(fs):
+            f, d = make_field(fs)
+            keep.append(d)
+            return f
+        for c in range(2):
+            ef.kin_a[c] = put(kin[c][0])
+            ef.kin_b[c] = put(kin[c][1])
+            ef.pot_a[c] = put(pot[c][0])
+            ef.pot_b[c] = put(pot[c][1])
+        ef.cpl = put(cpl)
+        check(load().sgpe_set_energy_fields(self._h, int(slot), ctypes.byref(ef)))
+
+    def energy(self, torch, slot, psik, out):
+        """FP64 energy of psik (device tensors) into ``out`` (10 doubles,
+        device)."""
+        check(load().sgpe_energy(self._h, int(slot), _ptr(psik[0]), _ptr(psik[1]),
+                                 _ptr(out), _stream(torch, psik[0].device)))
 
     def fft2(self, torch, inp, out, inverse, scale):
         check(load().sgpe_fft2(self._h, _ptr(inp[0]), _ptr(inp[1]),

@@ -112,6 +112,27 @@ def value_op(values, nx):
     return _spec(vals, kind, nx)
 
 
+def zero():
+    return FieldSpec(np.zeros(1, dtype=np.complex128), 0, 0)
+
+
+def energy_pair(energy):
+    """A real FP64 energy field as two specs whose sum is the field: one
+    compressed spec and zero when it is constant along an axis, an x-table
+    plus a y-table when it is separable (a(x) + b(y) to 8 ulp), else the
+    full field and zero."""
+    e = np.asarray(energy, dtype=np.float64)
+    nx = e.shape[1]
+    kind, vals = _axes_profile(e)
+    if kind is not None:
+        return _spec(vals, kind, nx), zero()
+    sep = split_separable(e)
+    if sep is not None:
+        a, b = sep
+        return _spec(a, 'x', nx), _spec(b, 'y', nx)
+    return _spec(e, 'full', nx), zero()
+
+
 def natural_order(k_field):
     """Centred (fftshift) k-space field -> natural FFT order."""
     return np.fft.ifftshift(np.asarray(k_field))

@@ -193,6 +193,7 @@ class TensorPropagator:
         self._plan.set_substep(1, spec_in)
         self.eng_out = SubstepOperators(self, 0, spec_out)
         self.eng_in = SubstepOperators(self, 1, spec_in)
+        self._set_energy_fields()
         self._psik_cache = None
         self.psik = [torch.as_tensor(p, dtype=self._ctype, device=self._device)
                      for p in psik0]
@@ -313,37 +314,64 @@ class TensorPropagator:
         return prop_result.PropResult(psi, psik, energy, pops, file_name)
 
     # --------------------------------------------------------------- energy
+    ENERGY_KEYS = ('kin', 'pot', 'int', 'cpl', 'total', 'mu', 'atoms_k',
+                   'atoms_r', 's1', 's2')
+
+    def _set_energy_fields(self):
+        """Slot 0: the energy of the propagated Hamiltonian (K_c as
+        propagated, V_c, coupling h = (Omega/2) exp(-i theta)).  Slot 1: the
+        original's reporting convention (tensor_propagator.py:308-324):
+        free kinetic energy plus kL kx with coupling, h = Omega/2."""
+        kin0 = [ops.energy_pair(k) for k in self._kin_np]
+        pot = [ops.energy_pair(v) for v in self._pot_np]
+        theta = 0.0 if self._expon_np is None else self._expon_np
+        nx = self._shape[1]
+        cpl0 = ops.value_op(self._coupling_np / 2 * np.exp(-1.0j * theta), nx)
+        self._plan.set_energy_fields(0, kin0, pot, cpl0)
+        if self._kx_np is not None and self._ky_np is not None:
+            k_ref = (self._kx_np**2 + self._ky_np**2) / 2
+            if self.is_coupling:
+                k_ref = k_ref + self.kL_recoil * self._kx_np
+            kin1 = [ops.energy_pair(k_ref)] * 2
+            cpl1 = ops.value_op(self._coupling_np / 2 + 0j, nx)
+            self._plan.set_energy_fields(1, kin1, pot, cpl1)
+            self._has_ref_energy = True
+        else:
+            self._has_ref_energy = False
+
+    def _energy_values(self, slot, psik=None):
+        if psik is None:
+            psik = self.psik
+        psik = [torch.as_tensor(p, device=self._device).to(self._ctype)
+                .contiguous() for p in psik]
+        out = torch.empty(10, dtype=torch.float64, device=self._device)
+        self._plan.energy(torch, slot, psik, out)
+        return out.cpu().numpy()
+
+    def energy(self, psik=None):
+        """FP64 energy functional of ``psik`` (default: the current state),
+        computed on the device: kinetic (spectral, with the propagated K_c),
+        potential, interaction (g_ij/2 n_i n_j), coupling, total, chemical
+        potential mu and the atom numbers in k- and real space."""
+        vals = self._energy_values(0, psik)
+        return dict(zip(self.ENERGY_KEYS, (float(v) for v in vals)))
+
     def eng_expect(self, psik):
         """[E_tot, E_kin, E_pot, E_int] in the convention of
         ``tensor_propagator.py:273-324`` (grid sums without the area
-        element).  The kinetic term
-        sum(|grad sqrt(n)|^2 + n |grad phi|^2 + 2 kL n d_x phi) / 2 is
-        evaluated spectrally as sum_k ((kx^2+ky^2)/2 + kL kx) |psik|^2 dv_k / dv_r
-        (the kL term only with coupling), which needs no phase unwrapping."""
+        element, interaction without the 1/2, coupling without the Raman
+        phase).  The kinetic term sum(|grad sqrt(n)|^2 + n |grad phi|^2
+        + 2 kL n d_x phi)/2 is evaluated spectrally as
+        sum_k ((kx^2+ky^2)/2 + kL kx) |psik|^2 dv_k / dv_r (the kL term only
+        with coupling), which needs no phase unwrapping."""
         assert len(psik) == 2, ("Requires two spinor components to calculate "
                                 "the energy expectation value.")
-        if isinstance(psik[0], np.ndarray):
-            psik = [torch.as_tensor(p, device=self._device).to(self._ctype)
-                    for p in psik]
+        if not self._has_ref_energy:
+            raise ValueError('eng_expect needs the k-space meshes of the '
+                             'PSpinor (space kx_mesh / ky_mesh)')
+        v = self._energy_values(1, psik)
         dv_r = float(self._space_np['dv_r'])
-        dv_k = float(self._space_np['dv_k'])
-        f64 = torch.float64
-        kx = torch.as_tensor(self._kx_np, dtype=f64, device=self._device)
-        ky = torch.as_tensor(self._ky_np, dtype=f64, device=self._device)
-        kin_density = (kx**2 + ky**2) / 2
-        if self.is_coupling:
-            kin_density = kin_density + self.kL_recoil * kx
-        densk = [(torch.abs(p)**2).to(f64) for p in psik]
-        kin = float(sum((kin_density * d).sum() for d in densk)) * dv_k / dv_r
-        psi = ttools.ifft_2d(psik, self._space_np['dr'])
-        dens = [(torch.abs(p)**2).to(f64) for p in psi]
-        pot = float(sum((torch.as_tensor(v, device=self._device) * d).sum()
-                        for v, d in zip(self._pot_np, dens)))
-        g = self.g_sc
-        int_e = float((g['uu'] * dens[0]**2 + g['dd'] * dens[1]**2
-                       + g['ud'] * dens[0] * dens[1]).sum())
-        cross = (torch.conj(psi[0]) * psi[1]).to(torch.complex128)
-        coupl = float((2 * cross.real * torch.as_tensor(
-            self._coupling_np, device=self._device) / 2).sum())
-        total = kin + pot + int_e + coupl
-        return [total, kin, pot, int_e]
+        kin, pot = v[0] / dv_r, v[1] / dv_r
+        int_e = (v[8] + v[9]) / dv_r
+        cpl = v[3] / dv_r
+        return [kin + pot + int_e + cpl, kin, pot, int_e]

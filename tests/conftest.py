@@ -40,6 +40,11 @@ def load_cases():
     return out
 
 
+def prop_case_names(cases):
+    """Names of the propagation cases (entries with run parameters)."""
+    return sorted(k for k, v in cases.items() if 'scalars' in v)
+
+
 def case_params(case):
     sc = case['scalars']
     return dict(dt=float(sc[4]), n_steps=int(sc[5]), dtype=int(sc[6]),

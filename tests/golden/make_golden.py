@@ -11,8 +11,9 @@ package (``spinor_gpe/pspinor/tensor_tools.py:7``,
 ``spinor_gpe/pspinor/plotting_tools.py:7-8``,
 ``spinor_gpe/pspinor/prop_result.py:8-10``) but are not installed here, so
 empty stand-in modules are registered first.  Nothing on the propagation path
-uses them; ``unwrap_phase`` is only reached through ``eng_expect``, which the
-fixtures do not record.
+uses them.  ``unwrap_phase`` is reached only through ``eng_expect``, which is
+recorded once, on a phase-smooth ground state, with the identity as
+``unwrap_phase`` (exact when no phase wraps).
 
 Each propagation case builds its problem with the shared recipe in
 ``spinor-gpe_gb300/spinor_gpe/workloads.py`` through the original ``PSpinor``
@@ -193,6 +194,21 @@ def main():
         out[pre + 'psik_final'] = np.array([p.numpy() for p in prop.psik])
         out[pre + 'pops'] = pops
         print(f'{name}: {n_steps} steps, final pops {pops[-1]}')
+
+    # The original energy convention on a phase-smooth ground state: with no
+    # phase wraps, an identity stand-in for scikit-image's unwrap_phase gives
+    # the original's eng_expect exactly (tensor_propagator.py:273-324).
+    import skimage.restoration as _rest
+    _rest.unwrap_phase = lambda a: a
+    kw, time, dt, n_steps, _, _ = all_cases['imag_plain_32']
+    ps = wl.build(rspin.PSpinor, rtt.fft_2d, os.path.join(tmp, 'energy') + '/', **kw)
+    prop = rtp.TensorPropagator(ps, dt, n_steps, 'cpu', time=time)
+    for _ in range(n_steps):
+        prop.full_step()
+    out['energy/psik'] = np.array([p.numpy() for p in prop.psik])
+    out['energy/kx_mesh'] = ps.space['kx_mesh']
+    out['energy/ky_mesh'] = ps.space['ky_mesh']
+    out['energy/eng_expect'] = np.array(prop.eng_expect(prop.psik))
 
     # FFT helpers on a random non-square pair (tensor_tools.py:201-258)
     rng = np.random.default_rng(5)

@@ -14,14 +14,14 @@ import numpy as np
 import pytest
 import torch
 
-from conftest import case_params, load_cases, rel_l2, spin_from_case
+from conftest import prop_case_names, case_params, load_cases, rel_l2, spin_from_case
 from oracle import OraclePropagator, OracleInputs, calc_pops
 
 pytestmark = pytest.mark.gpu
 
 TOL = {128: 1e-10, 64: 1e-5}
 CASES = load_cases()
-PROP_CASES = sorted(k for k in CASES if k != 'fft')
+PROP_CASES = prop_case_names(CASES)
 
 
 @pytest.fixture(scope='module')
@@ -300,3 +300,45 @@ def test_complex64_error_not_worse_than_reference_complex64(tp, tmp_path, name):
     prop.full_steps(n)
     got = np.array([t.cpu().numpy() for t in prop.psik])
     assert rel_l2(got, ref128) <= bar
+
+
+@pytest.mark.parametrize('name', ['imag_plain_32', 'imag_raman_64x32',
+                                  'real_raman_32', 'imag_gradients_32',
+                                  'real_bump_32', 'real_rot_32x64'])
+@pytest.mark.parametrize('dtype', [128, 64])
+def test_device_energy_matches_oracle(tp, tmp_path, name, dtype):
+    """FP64 energy functional on the device vs the oracle's NumPy FP64
+    evaluation of the same functional on the same state."""
+    from oracle.energy import energy_functional
+    case = CASES[name]
+    p = case_params(case)
+    prop = tp.TensorPropagator(spin_from_case(case, tmp_path), p['dt'],
+                               p['n_steps'], 'cuda', time=p['time'],
+                               dtype=dtype)
+    prop.full_steps(3)
+    psik = [t.cpu().numpy().astype(np.complex128) for t in prop.psik]
+    sc = case['scalars']
+    theta = 0.0 if bool(sc[2]) else 2 * sc[1] * case['x_mesh']
+    ref = energy_functional(psik, case['kin_eng_spin'], case['pot_eng_spin'],
+                            case['coupling'], theta, case['g'], case['dr'],
+                            case['dv'][0], case['dv'][1])
+    got = prop.energy()
+    vals = np.array([got[k] for k in prop.ENERGY_KEYS])
+    tol = 1e-11 if dtype == 128 else 2e-6
+    scale = np.maximum(np.abs(ref), abs(ref[4]))
+    assert np.all(np.abs(vals - ref) <= tol * scale), (vals, ref)
+
+
+def test_eng_expect_matches_reference_convention(tp, tmp_path):
+    """The drop-in eng_expect reproduces the original's potential and
+    interaction terms exactly on the golden ground state, and its total to
+    the finite-difference truncation of the original's kinetic term."""
+    e = CASES['energy']
+    case = CASES['imag_plain_32']
+    spin = spin_from_case(case, tmp_path)
+    prop = tp.TensorPropagator(spin, 0.02, 1, 'cuda', time='imag', dtype=128)
+    got = prop.eng_expect([torch.as_tensor(p, device='cuda') for p in e['psik']])
+    ref = e['eng_expect']
+    np.testing.assert_allclose(got[2:], ref[2:], rtol=1e-11)
+    assert abs(got[1] - ref[1]) / ref[1] < 0.03
+    assert abs(got[0] - ref[0]) / ref[0] < 1e-3

@@ -10,7 +10,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, case_params, load_cases
+from conftest import prop_case_names, GOLDEN, case_params, load_cases
 from oracle import OraclePropagator, inputs_from_arrays
 from spinor_gpe import workloads
 from spinor_gpe.pspinor import operators as ops
@@ -83,7 +83,7 @@ def test_pspinor_errors(tmp_path):
         ps.shift_momentum()
 
 
-@pytest.mark.parametrize('name', sorted(k for k in CASES if k != 'fft'))
+@pytest.mark.parametrize('name', prop_case_names(CASES))
 def test_operator_specs_reproduce_dense_operators(name):
     case = CASES[name]
     p = case_params(case)

@@ -11,12 +11,12 @@ import numpy as np
 import pytest
 import torch
 
-from conftest import case_params, load_cases, rel_l2
+from conftest import prop_case_names, case_params, load_cases, rel_l2
 from oracle import (OraclePropagator, calc_pops, fft_1d, fft_2d, ifft_1d,
                     ifft_2d, inputs_from_arrays)
 
 CASES = load_cases()
-PROP_CASES = sorted(k for k in CASES if k != 'fft')
+PROP_CASES = prop_case_names(CASES)
 
 
 @pytest.mark.parametrize('name', PROP_CASES)
@@ -73,3 +73,21 @@ def test_oracle_fft_invariants(shape):
     vol = 4 * np.pi**2 / n                  # compare_norm_torch (:453-472)
     atoms_k = sum(calc_pops(grid_k, vol))
     assert abs(atoms[0] - atoms_k) <= eps * n
+
+
+def test_oracle_energy_convention_matches_reference():
+    """The original's eng_expect on a phase-smooth ground state (golden,
+    recorded with an identity phase unwrap, exact without wraps): potential
+    and interaction terms agree exactly; the spectral kinetic term agrees with
+    the original's finite differences to their O(dx^2) truncation (dx = 0.25)."""
+    from oracle.energy import reference_convention
+    e = CASES['energy']
+    c = CASES['imag_plain_32']
+    sc = c['scalars']
+    got = reference_convention(e['psik'], e['kx_mesh'], e['ky_mesh'], sc[1],
+                               bool(sc[3]), c['pot_eng_spin'], c['coupling'],
+                               c['g'], c['dr'], c['dv'][0], c['dv'][1])
+    ref = e['eng_expect']
+    np.testing.assert_allclose(got[2:], ref[2:], rtol=1e-12)
+    assert abs(got[1] - ref[1]) / ref[1] < 0.03
+    assert abs(got[0] - ref[0]) / ref[0] < 1e-3

@@ -1,0 +1,142 @@
+"""Full-length validation of the solver on the named problem set-ups.
+
+Test infrastructure (needs a CUDA GPU; not collected by pytest): each
+set-up is run through the drop-in propagator and through the oracle, the
+original algorithm restated in torch, here executed on the GPU in complex128.
+Printed per set-up as one JSON line: relative L2 error of the final psik,
+energy / chemical potential / atom number of both (FP64 functional), the
+solver's steps/s.
+
+    python tests/validate_configs.py [ground_state_256 raman_quench_1024 vortex_2048]
+
+* ground_state_256: 256^2, complex128, 1000 imaginary steps, dt = 0.02.
+* raman_quench_1024: 1024^2, complex64, 3000 imaginary steps at dt = 0.01,
+  then delta 0 -> 0.5 and 10000 real steps at dt = 1e-3; real-time energy
+  drift of both.
+* vortex_2048: 2048^2, complex64 (and complex128), 2000 imaginary steps at
+  dt = 0.01, 8 seeded vortices.
+"""
+import json
+import os
+import sys
+import tempfile
+import time
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+for p in (os.path.join(REPO, 'spinor-gpe_gb300'), REPO):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+from oracle import OracleInputs, OraclePropagator          # noqa: E402
+from oracle.energy import energy_functional                # noqa: E402
+from spinor_gpe import workloads                           # noqa: E402
+from spinor_gpe.pspinor import pspinor as spin             # noqa: E402
+from spinor_gpe.pspinor import tensor_propagator as tprop  # noqa: E402
+from spinor_gpe.pspinor import tensor_tools as ttools      # noqa: E402
+
+
+def inputs(ps):
+    return OracleInputs(
+        psik=[np.asarray(p) for p in ps.psik],
+        kin_eng_spin=[np.asarray(k) for k in ps.kin_eng_spin],
+        pot_eng_spin=[np.asarray(v) for v in ps.pot_eng_spin],
+        coupling=np.asarray(ps.coupling, dtype=np.float64),
+        x_mesh=ps.space['x_mesh'], dr=ps.space['dr'],
+        dv_r=float(ps.space['dv_r']), dv_k=float(ps.space['dv_k']),
+        g_sc=dict(ps.g_sc), atom_num=float(ps.atom_num),
+        kL_recoil=float(ps.kL_recoil), rot_coupling=bool(ps.rot_coupling),
+        is_coupling=bool(ps.is_coupling))
+
+
+def oracle_energy(ps, psik):
+    theta = 0.0 if ps.rot_coupling else 2 * ps.kL_recoil * ps.space['x_mesh']
+    g = (ps.g_sc['uu'], ps.g_sc['dd'], ps.g_sc['ud'])
+    return energy_functional(psik, ps.kin_eng_spin, ps.pot_eng_spin,
+                             np.asarray(ps.coupling, dtype=np.float64), theta, g,
+                             ps.space['dr'], float(ps.space['dv_r']),
+                             float(ps.space['dv_k']))
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm((np.asarray(a) - np.asarray(b)).ravel())
+                 / np.linalg.norm(np.asarray(b).ravel()))
+
+
+def run_solver(ps, dt, n, time_mode, dtype):
+    prop = tprop.TensorPropagator(ps, dt, n, 'cuda', time=time_mode, dtype=dtype)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    prop.full_steps(n)
+    psik = [p.cpu().numpy().astype(np.complex128) for p in prop.psik]
+    dt_s = time.perf_counter() - t0
+    return prop, psik, n / dt_s
+
+
+def run_oracle(ps, dt, n, time_mode):
+    orc = OraclePropagator(inputs(ps), dt, time_mode, 128, device='cuda')
+    for _ in range(n):
+        orc.full_step()
+    return orc.psik_numpy()
+
+
+def summary(name, ps, mine, ref, rate, extra=None):
+    em = oracle_energy(ps, mine)
+    er = oracle_energy(ps, ref)
+    out = {'config': name, 'psik_rel_l2': rel_l2(mine, ref),
+           'energy': em[4], 'energy_oracle': er[4],
+           'energy_rel_err': abs(em[4] - er[4]) / abs(er[4]),
+           'mu': em[5], 'mu_oracle': er[5], 'mu_rel_err': abs(em[5] - er[5]) / abs(er[5]),
+           'atoms': em[7], 'atoms_oracle': er[7], 'steps_per_s': rate}
+    if extra:
+        out.update(extra)
+    print(json.dumps(out), flush=True)
+
+
+def ground_state_256(tmp):
+    ps = workloads.ground_state_256(spin.PSpinor, ttools.fft_2d, tmp + '/c1/')
+    _, mine, rate = run_solver(ps, 0.02, 1000, 'imag', 128)
+    ref = run_oracle(ps, 0.02, 1000, 'imag')
+    summary('ground_state_256 (complex128, 1000 imaginary steps)', ps, mine,
+            ref, rate)
+
+
+def raman_quench_1024(tmp):
+    ps = workloads.raman_quench_1024(spin.PSpinor, ttools.fft_2d, tmp + '/c2/')
+    prop, mine_g, rate_i = run_solver(ps, 0.01, 3000, 'imag', 64)
+    ref_g = run_oracle(ps, 0.01, 3000, 'imag')
+    ground_err = rel_l2(mine_g, ref_g)
+    # quench from the same (oracle) ground state for both
+    ps.psik = list(ref_g)
+    ps.detuning_uniform(0.5)
+    e0 = oracle_energy(ps, ref_g)[4]
+    prop, mine, rate = run_solver(ps, 1e-3, 10000, 'real', 64)
+    ref = run_oracle(ps, 1e-3, 10000, 'real')
+    summary('raman_quench_1024 (complex64, 3000 imag + 10000 real steps)', ps,
+            mine, ref, rate,
+            {'ground_state_psik_rel_l2': ground_err, 'imag_steps_per_s': rate_i,
+             'energy_drift_solver': (oracle_energy(ps, mine)[4] - e0) / abs(e0),
+             'energy_drift_oracle': (oracle_energy(ps, ref)[4] - e0) / abs(e0)})
+
+
+def vortex_2048(tmp):
+    ps = workloads.vortex_2048(spin.PSpinor, ttools.fft_2d, tmp + '/c3/')
+    ref = run_oracle(ps, 0.01, 2000, 'imag')
+    for dtype in (64, 128):
+        _, mine, rate = run_solver(ps, 0.01, 2000, 'imag', dtype)
+        summary(f'vortex_2048 (complex{dtype}, 2000 imaginary steps)', ps, mine,
+                ref, rate)
+
+
+CONFIGS = {'ground_state_256': ground_state_256,
+           'raman_quench_1024': raman_quench_1024,
+           'vortex_2048': vortex_2048}
+
+if __name__ == '__main__':
+    names = sys.argv[1:] or list(CONFIGS)
+    tmp = tempfile.mkdtemp(prefix='sgpe_validate_')
+    for n in names:
+        CONFIGS[n](tmp)

@@ -50,9 +50,22 @@ def parse():
     ap.add_argument('--steps', type=int, default=1000)
     ap.add_argument('--warmup', type=int, default=10)
     ap.add_argument('--impl', default='native', choices=['native', 'reference'])
-    ap.add_argument('--n', type=int, default=1024, help='grid side')
+    ap.add_argument('--grid', '--n', dest='n', type=int, default=1024,
+                    help='grid side')
     ap.add_argument('--prep-steps', type=int, default=3000)
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--workload', default='raman_quench',
+                    choices=['raman_quench', 'batched_uneven', 'served'],
+                    help='raman_quench (headline); batched_uneven (independent '
+                         'ground states stepped as one batch against the same '
+                         'solves run one after another); served (a Poisson '
+                         'request stream through the continuous-batching loop '
+                         'against the same requests solved one after another)')
+    ap.add_argument('--solves', type=int, default=96)
+    ap.add_argument('--batch-steps', type=int, default=2000)
+    ap.add_argument('--serve-rate', type=float, default=200.0)
+    ap.add_argument('--serve-window', type=float, default=0.5)
+    ap.add_argument('--max-active', type=int, default=64)
     return ap.parse_args()
 
 
@@ -359,6 +372,170 @@ def run_native(args, world, rank, local):
         print(json.dumps(line))
 
 
+# ---------------------------------------------------- batched uneven solves
+
+def run_batched(args, world, rank, local):
+    """Independent imaginary-time ground states with uneven grids (sides
+    128..1024, dx = 0.125) and seeded parameters, complex64, dt = 0.02: all
+    solves advanced together through ``PropagatorBatch`` (one CUDA graph with
+    a branch per solve), against the plain single-solve drop-in stepping the
+    same solves one after another.  Metric: aggregate grid-point-steps/s."""
+    import torch
+    from spinor_gpe import workloads
+    from spinor_gpe.batch import PropagatorBatch
+    from spinor_gpe.pspinor import pspinor as spin
+    from spinor_gpe.pspinor import tensor_propagator as tprop
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    torch.cuda.set_device(local)
+    device = f'cuda:{local}'
+    tmp = tempfile.mkdtemp(prefix='sgpe_batch_')
+    spins = workloads.batched_uneven(spin.PSpinor, ttools.fft_2d, tmp + '/',
+                                     n_solves=args.solves, seed=4 + rank)
+    k = args.batch_steps
+    props = [tprop.TensorPropagator(s, 0.02, k, device, time='imag', dtype=64)
+             for s in spins]
+    points = sum(s.psik[0].size for s in spins)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        barrier(world)
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        return max_over_ranks(ev0.elapsed_time(ev1) / 1e3, world)
+
+    # plain solves one after another (warm-up captures each plan's graphs)
+    for p in props:
+        p.full_steps(max(args.warmup, 9))
+    t_seq = timed(lambda: [p.full_steps(k) for p in props])
+
+    batch = PropagatorBatch(props)
+    batch.full_steps(max(args.warmup, 9))
+    with ClockSampler(local) as clk:
+        t_bat = timed(lambda: batch.full_steps(k))
+    for p in props[:4]:
+        assert all(torch.isfinite(c).all().item() for c in p.psik)
+    sizes = {}
+    for s in spins:
+        sizes[s.psik[0].shape[0]] = sizes.get(s.psik[0].shape[0], 0) + 1
+    value = world * points * k / t_bat
+    seq = world * points * k / t_seq
+    line = {
+        'metric': 'grid-point-steps/s, batched uneven imaginary-time solves '
+                  '(complex64)',
+        'value': value, 'unit': 'grid-point-steps/s', 'n_gpus': world,
+        'steps': k, 'warmup': max(args.warmup, 9), 'ms_per_step': 1e3 * t_bat / k,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'c64 (fp32 butterflies; fp64 reductions)',
+        'data': 'synthetic (seeded sizes and parameters, Thomas-Fermi + '
+                'phase noise)',
+        'config': {'workload': f'batched_uneven_{args.solves}',
+                   'solves_per_gpu': args.solves, 'grid_sides': sizes,
+                   'grid_points_per_gpu': points, 'dt': 0.02, 'time': 'imag',
+                   'l2': f'inputs larger than L2: {points * 16 >> 20} MiB of '
+                         f'state per GPU',
+                   'parallelism': f'replicas x{world}'},
+        'sequential_plain': {'value': seq, 'unit': 'grid-point-steps/s',
+                             'what': 'the same solves, each advanced alone '
+                                     'with TensorPropagator.full_steps'},
+        'speedup_vs_sequential': value / seq,
+        'gpu_launches': 6 * k * args.solves,
+        'clocks': clk.summary(),
+    }
+    batch.close()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+# ------------------------------------------------------ served request stream
+
+def run_served(args, world, rank, local):
+    """A seeded Poisson request stream (70% ground states at 256^2/512^2 run
+    to |dE| < 1e-8 per step or 3000 steps, 30% real-time quenches at 1024^2
+    for 5000 steps; complex64) served by the continuous-batching loop under
+    a 150 GB admission cap, then the same requests solved one after another
+    by the plain drop-in.  Reports latency percentiles (arrival to result),
+    offered and served load, aggregate grid-point-steps/s of both."""
+    import torch
+    from spinor_gpe import serve, workloads
+    torch.cuda.set_device(local)
+    device = f'cuda:{local}'
+    tmp = tempfile.mkdtemp(prefix='sgpe_serve_')
+    stream = workloads.served_stream(rate=args.serve_rate,
+                                     window=args.serve_window, seed=5 + rank)
+    reqs = serve.requests_from_stream(stream, tmp + '/', device=device)
+    offered_max = sum(r.max_steps * r.grid_points for r in reqs)
+    # warm-up: one small solve through the loop (library load, first graphs)
+    serve.SolveServer(device, max_active=2).run(reqs[:1], realtime=False)
+    barrier(world)
+    torch.cuda.synchronize()
+    srv = serve.SolveServer(device, hbm_cap=150e9, max_active=args.max_active)
+    with ClockSampler(local) as clk:
+        res = srv.run(reqs, realtime=True)
+    st = dict(srv.stats)
+    wall = max_over_ranks(st['wall_s'], world)
+    barrier(world)
+    seq, t_seq = serve.run_sequential(reqs, device)
+    t_seq = max_over_ranks(t_seq, world)
+    same = all((a.steps, a.converged) == (b.steps, b.converged)
+               for a, b in zip(sorted(res, key=lambda r: r.rid), seq))
+    gps = st['grid_point_steps']
+    kinds = {}
+    for r in res:
+        k = kinds.setdefault(f'{r.kind}_{int(round(r.grid_points ** 0.5))}',
+                             {'n': 0, 'steps': 0, 'converged': 0, 'lat': []})
+        k['n'] += 1
+        k['steps'] += r.steps
+        k['converged'] += int(r.converged)
+        k['lat'].append(r.latency)
+    for k in kinds.values():
+        lat = np.array(k.pop('lat'))
+        k['p50_ms'] = float(np.percentile(lat, 50) * 1e3)
+        k['p99_ms'] = float(np.percentile(lat, 99) * 1e3)
+    line = {
+        'metric': 'served request stream: p50/p99 latency (ms) and aggregate '
+                  'grid-point-steps/s (complex64)',
+        'value': world * gps / wall, 'unit': 'grid-point-steps/s',
+        'p50_ms': st['p50_ms'], 'p99_ms': st['p99_ms'],
+        'n_gpus': world, 'steps': len(res), 'warmup': 1,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'c64 (fp32 butterflies; fp64 reductions)',
+        'data': 'synthetic (seeded Poisson stream; Thomas-Fermi starts)',
+        'config': {'workload': f'served_stream_{args.serve_rate:g}rps_'
+                               f'{args.serve_window:g}s',
+                   'requests': len(res), 'rate_per_s': args.serve_rate,
+                   'window_s': args.serve_window, 'hbm_cap_bytes': 150e9,
+                   'max_active': args.max_active,
+                   'parallelism': f'replicas x{world}'},
+        'offered': {'requests_per_s': args.serve_rate,
+                    'grid_point_steps_upper_bound': offered_max,
+                    'grid_point_steps_per_s_upper_bound':
+                        offered_max / args.serve_window},
+        'served': {'grid_point_steps': gps, 'wall_s': wall,
+                   'requests_per_s': len(res) / wall,
+                   'peak_active': st['peak_active'],
+                   'peak_admitted_bytes': st['peak_admitted_bytes'],
+                   'by_kind': kinds},
+        'sequential_plain': {'value': world * gps / t_seq,
+                             'unit': 'grid-point-steps/s',
+                             'device_s': t_seq,
+                             'what': 'the same requests with the same stopping '
+                                     'rules, each solved alone by the plain '
+                                     'drop-in (device time of the stepping; '
+                                     'host set-up excluded)'},
+        'speedup_vs_sequential': t_seq / wall,
+        'same_steps_alone_and_in_mix': same,
+        'clocks': clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
 # ------------------------------------------------------------ reference arm
 
 def run_reference(args, world, rank, local):
@@ -398,6 +575,10 @@ def main():
     world, rank, local = dist_setup()
     if args.impl == 'reference':
         run_reference(args, world, rank, local)
+    elif args.workload == 'batched_uneven':
+        run_batched(args, world, rank, local)
+    elif args.workload == 'served':
+        run_served(args, world, rank, local)
     else:
         run_native(args, world, rank, local)
     if world > 1:

@@ -75,8 +75,8 @@ int sgpe_version(void);
 /* Message of the last failing call on this thread ("" if none). */
 const char* sgpe_last_error(void);
 
-/* Create a plan for an (ny, nx) grid.  Sizes: powers of two, 32..4096 on
- * each axis.  dtype_bits: 64 (complex64) or 128 (complex128).  Allocates the
+/* Create a plan for an (ny, nx) grid.  Sizes on each axis: powers of two
+ * 32..4096, or 192, 384, 768 (3 * 2^k, with a radix-3 stage).  dtype_bits: 64 (complex64) or 128 (complex128).  Allocates the
  * device state on `device`.  Synchronous.
  * Replaces: TensorPropagator.__init__ tensor uploads
  * (spinor_gpe/pspinor/tensor_propagator.py:111-122). */
@@ -172,6 +172,23 @@ int sgpe_energy(sgpe_plan* plan, int slot, const void* psik0, const void* psik1,
  * most one step to reach the graph's steady state).
  * Instrumentation of the native path; no counterpart in the original. */
 int sgpe_time_passes(sgpe_plan* plan, int n_steps, double* col_ms, double* row_ms, void* stream);
+
+/* A batch of plans stepped together (many independent solves, uneven grid
+ * sizes and parameters).  The plans stay owned by the caller and must
+ * outlive the batch; they must be on one device and not be stepped through
+ * other calls while the batch exists.  No counterpart in the original
+ * (which runs one solve per process). */
+typedef struct sgpe_batch sgpe_batch;
+int sgpe_batch_create(sgpe_batch** batch, sgpe_plan* const* plans, int n_plans);
+int sgpe_batch_destroy(sgpe_batch* batch);
+
+/* Advance every plan of the batch by n_steps full steps (no populations).
+ * The solves' steady-state steps are captured once as independent branches
+ * of a CUDA graph (one graph per 8 steps and one per step) and replayed on
+ * `stream`, so their kernels run concurrently on the GPU.  Plans that are not
+ * in the steady state first take one eager step.  Results are identical to
+ * stepping each plan alone with sgpe_full_steps. */
+int sgpe_batch_steps(sgpe_batch* batch, int n_steps, void* stream);
 
 /* Size in bytes of the device scratch array used by sgpe_fft2_static
  * (2.25 MiB, present on every GPU that loads the library). */

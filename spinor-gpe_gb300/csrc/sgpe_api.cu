@@ -134,6 +134,18 @@ namespace {
 constexpr int kGraphSteps = 8;
 }
 
+// A set of plans stepped together: their steady-state steps are captured as
+// independent branches of one CUDA graph, so the solves' kernels run
+// concurrently (sgpe_batch_steps).
+struct sgpe_batch {
+  std::vector<sgpe_plan*> plans;
+  int device = 0;
+  cudaStream_t root = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> joins;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // 1 step, kGraphSteps steps
+};
+
 namespace {
 
 // Per-stage twiddle table of an (n, e) transform, in the order the FFT
@@ -145,7 +157,7 @@ template <typename R> void* upload_twiddles(int n, int e, cudaError_t* err) {
   std::vector<C> h;
   const double two_pi = 6.283185307179586476925286766559;
   for (int ns = 1; ns < n;) {
-    const int rs = (n / ns < e) ? n / ns : e;
+    const int rs = sgpe::stage_radix(n, e, ns);
     const long long len = (long long)ns * rs;
     for (int r = 1; r < rs; ++r)
       for (int k = 0; k < ns; ++k) {
@@ -642,7 +654,7 @@ int sgpe_plan_create(sgpe_plan** out, int ny, int nx, int dtype_bits, int device
   if (out == nullptr) return fail(SGPE_ERR_ARG, "plan output pointer is null");
   *out = nullptr;
   if (!sgpe::size_supported(nx) || !sgpe::size_supported(ny))
-    return fail(SGPE_ERR_ARG, "grid sizes must be powers of two in [32, 4096], got ny=" + std::to_string(ny) +
+    return fail(SGPE_ERR_ARG, "grid sizes must be powers of two in [32, 4096] or 192, 384, 768, got ny=" + std::to_string(ny) +
                                   " nx=" + std::to_string(nx));
   if (dtype_bits != 64 && dtype_bits != 128) return fail(SGPE_ERR_ARG, "dtype_bits must be 64 or 128");
   DeviceGuard g(device);
@@ -947,6 +959,112 @@ int sgpe_time_passes(sgpe_plan* p, int n_steps, double* col_ms, double* row_ms, 
   if (e != cudaSuccess) return cuda_fail(e, "time_passes");
   *col_ms = tc / n_pass;
   *row_ms = tr / n_pass;
+  return SGPE_OK;
+}
+
+int sgpe_batch_create(sgpe_batch** out, sgpe_plan* const* plans, int n_plans) {
+  if (out == nullptr || plans == nullptr || n_plans < 1) return fail(SGPE_ERR_ARG, "null output/plans or no plans");
+  *out = nullptr;
+  for (int i = 0; i < n_plans; ++i) {
+    if (plans[i] == nullptr) return fail(SGPE_ERR_ARG, "null plan in batch");
+    if (plans[i]->device != plans[0]->device) return fail(SGPE_ERR_ARG, "batch plans must share a device");
+    for (int k = 0; k < i; ++k)
+      if (plans[k] == plans[i]) return fail(SGPE_ERR_ARG, "a plan appears twice in the batch");
+  }
+  DeviceGuard g(plans[0]->device);
+  sgpe_batch* b = new sgpe_batch();
+  b->plans.assign(plans, plans + n_plans);
+  b->device = plans[0]->device;
+  cudaError_t e = cudaStreamCreateWithFlags(&b->root, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  b->joins.assign(n_plans, nullptr);
+  for (int i = 0; i < n_plans && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&b->joins[i], cudaEventDisableTiming);
+  for (int i = 0; i < n_plans && e == cudaSuccess; ++i)
+    if (plans[i]->cap_stream == nullptr) e = cudaStreamCreateWithFlags(&plans[i]->cap_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    sgpe_batch_destroy(b);
+    return cuda_fail(e, "batch create");
+  }
+  *out = b;
+  return SGPE_OK;
+}
+
+int sgpe_batch_destroy(sgpe_batch* b) {
+  if (b == nullptr) return SGPE_OK;
+  DeviceGuard g(b->device);
+  for (auto& x : b->graph)
+    if (x) cudaGraphExecDestroy(x);
+  for (auto& ev : b->joins)
+    if (ev) cudaEventDestroy(ev);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->root) cudaStreamDestroy(b->root);
+  delete b;
+  return SGPE_OK;
+}
+
+namespace {
+// Capture `steps` steady-state steps of every plan as parallel branches.
+int capture_batch(sgpe_batch* b, int steps, cudaGraphExec_t* out) {
+  for (sgpe_plan* p : b->plans)
+    for (int x = 0; x < 2; ++x)
+      for (int y = 0; y < 2; ++y)
+        if (ensure_pair(p, x, y) != SGPE_OK) return SGPE_ERR_OOM;
+  cudaError_t e = cudaStreamBeginCapture(b->root, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return cuda_fail(e, "batch begin capture");
+  if (e == cudaSuccess) e = cudaEventRecord(b->fork, b->root);
+  int rc = SGPE_OK;
+  for (size_t i = 0; i < b->plans.size() && e == cudaSuccess && rc == SGPE_OK; ++i) {
+    sgpe_plan* p = b->plans[i];
+    e = cudaStreamWaitEvent(p->cap_stream, b->fork, 0);
+    for (int k = 0; k < steps && e == cudaSuccess && rc == SGPE_OK; ++k)
+      rc = p->bits == 64 ? eager_step<float>(p, nullptr, p->cap_stream) : eager_step<double>(p, nullptr, p->cap_stream);
+    if (e == cudaSuccess && rc == SGPE_OK) e = cudaEventRecord(b->joins[i], p->cap_stream);
+    if (e == cudaSuccess && rc == SGPE_OK) e = cudaStreamWaitEvent(b->root, b->joins[i], 0);
+  }
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(b->root, &graph);
+  if (e == cudaSuccess) e = e2;
+  if (rc != SGPE_OK || e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc != SGPE_OK ? rc : cuda_fail(e, "batch capture");
+  }
+  e = cudaGraphInstantiate(out, graph, 0);
+  cudaGraphDestroy(graph);
+  return e == cudaSuccess ? SGPE_OK : cuda_fail(e, "batch graph instantiate");
+}
+}  // namespace
+
+int sgpe_batch_steps(sgpe_batch* b, int n_steps, void* stream) {
+  if (b == nullptr) return fail(SGPE_ERR_ARG, "null batch");
+  if (n_steps < 0) return fail(SGPE_ERR_ARG, "n_steps must be non-negative");
+  for (sgpe_plan* p : b->plans) {
+    if (p->form == kEmpty) return fail(SGPE_ERR_STATE, "a batch plan has no state loaded");
+    if (!ready(p)) return fail(SGPE_ERR_STATE, "a batch plan has no physics or operators");
+  }
+  DeviceGuard g(b->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int done = 0;
+  // bring every plan to the steady state with one eager step (on `s`)
+  bool eager = false;
+  for (sgpe_plan* p : b->plans)
+    if (!(p->form == kMixed && p->prev_sub == 0 && p->pending_pops == nullptr)) eager = true;
+  if (eager && n_steps > 0) {
+    for (sgpe_plan* p : b->plans) {
+      const int rc = p->bits == 64 ? eager_step<float>(p, nullptr, s) : eager_step<double>(p, nullptr, s);
+      if (rc != SGPE_OK) return rc;
+    }
+    done = 1;
+  }
+  while (done < n_steps) {
+    const int k = (n_steps - done >= kGraphSteps) ? 1 : 0;
+    if (b->graph[k] == nullptr) {
+      const int rc = capture_batch(b, k ? kGraphSteps : 1, &b->graph[k]);
+      if (rc != SGPE_OK) return rc;
+    }
+    const cudaError_t e = cudaGraphLaunch(b->graph[k], s);
+    if (e != cudaSuccess) return cuda_fail(e, "batch graph launch");
+    done += k ? kGraphSteps : 1;
+  }
   return SGPE_OK;
 }
 

@@ -10,8 +10,9 @@
 // output is in natural order, which lets a kernel apply point-wise operators
 // between an inverse and a forward transform without any reordering.
 //
-// Stage s has radix R_s (E, E, ..., remainder) and sub-length Ns = prod of
-// the earlier radices.  A thread runs Q = E/R_s butterflies per stage on the
+// Stage s has radix R_s (E, E, ..., remainder; for N = 3 * 2^k power-of-two
+// radices then 3, see stage_radix) and sub-length Ns = prod of the earlier
+// radices.  A thread runs Q = E/R_s butterflies per stage on the
 // "virtual threads" vt = j + q*T; inputs are at vt + r*N/R, twiddle
 // W_N^{(vt mod Ns) * r * N/(Ns*R)}, outputs at (vt/Ns)*Ns*R + vt mod Ns + r*Ns.
 //
@@ -89,6 +90,21 @@ template <int DIR> struct Dft<2, DIR> {
     a[1] = csub(t, a[1]);
   }
 };
+template <int DIR> struct Dft<3, DIR> {
+  template <class C> __device__ __forceinline__ static void run(C* a) {
+    using R = decltype(C::x);
+    const R half = R(0.5);
+    const R s3 = R(0.86602540378443864676);  // sqrt(3)/2
+    const C t1 = cadd(a[1], a[2]);
+    const C t2 = csub(a[1], a[2]);
+    const C m = cmake<C>(a[0].x - half * t1.x, a[0].y - half * t1.y);
+    // +/- i DIR sqrt(3)/2 (a1 - a2)
+    const C r = crot<DIR>(cscale(t2, s3));
+    a[0] = cadd(a[0], t1);
+    a[1] = cadd(m, r);
+    a[2] = csub(m, r);
+  }
+};
 template <int DIR> struct Dft<4, DIR> {
   template <class C> __device__ __forceinline__ static void run(C* a) {
     C t0 = cadd(a[0], a[2]), t1 = csub(a[0], a[2]);
@@ -146,12 +162,27 @@ template <int DIR> struct Dft<16, DIR> {
   }
 };
 
+// Radix of the stage with sub-length NS of an (N, E) transform.  Powers of
+// two: E per stage, the remainder last.  N = 3 * 2^k: power-of-two stages of
+// at most P (the largest power of two dividing E), then one radix-3 stage.
+__host__ __device__ constexpr int stage_radix(int N, int E, int NS) {
+  const int m = N / NS;
+  if (m % 3 == 0) {
+    if (m == 3) return 3;
+    int p = 1;
+    while (E % (2 * p) == 0) p *= 2;
+    const int two = m / 3;
+    return two < p ? two : p;
+  }
+  return m < E ? m : E;
+}
+
 // Offset of the twiddle block of the stage with sub-length NS in the table
 // of an (N, E) transform; tw_offset(N, E, N) is the table length.
 __host__ __device__ constexpr int tw_offset(int N, int E, int NS) {
   int off = 0, ns = 1;
   while (ns < NS) {
-    const int r = (N / ns < E) ? N / ns : E;
+    const int r = stage_radix(N, E, ns);
     off += (r - 1) * ns;
     ns *= r;
   }
@@ -179,7 +210,7 @@ template <class C, int E> struct LineSmem {
 template <int N, int E, int DIR, int L, int NS, bool FROM_SMEM, bool TO_SMEM, class C, class SM>
 __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, const C* __restrict__ tw) {
   constexpr int T = N / E;
-  constexpr int R = (N / NS < E) ? (N / NS) : E;
+  constexpr int R = stage_radix(N, E, NS);
   constexpr int Q = E / R;
   constexpr bool kFirst = (NS == 1);
   constexpr bool kLast = (NS * R == N);

@@ -1,7 +1,8 @@
 // Launch configuration and size dispatch for the split-step kernels.
 //
-// Line lengths are compile-time: every power of two from 32 to 4096 along
-// either axis is instantiated for complex64 (float) and complex128 (double).
+// Line lengths are compile-time: every power of two from 32 to 4096, and 192,
+// 384 and 768, along either axis, instantiated for complex64 (float) and
+// complex128 (double).
 #pragma once
 #include "sgpe_kernels.cuh"
 
@@ -44,8 +45,14 @@ template <> struct Tune<double> {
 constexpr int cmin(int a, int b) { return a < b ? a : b; }
 constexpr int cmax(int a, int b) { return a > b ? a : b; }
 
+// Points per thread: the tuned E for powers of two; 24 (complex64) or 12
+// (complex128) for N = 3 * 2^k, so that every stage radix divides it.
+template <typename R> constexpr int pick_e(int n, int e_pow2) {
+  return (n % 3 == 0) ? (sizeof(R) == 4 ? 24 : 12) : cmin(n, e_pow2);
+}
+
 template <typename R, int N> struct RowCfg {
-  static constexpr int E = cmin(N, Tune<R>::ROW_E);
+  static constexpr int E = pick_e<R>(N, Tune<R>::ROW_E);
   static constexpr int T = N / E;
   // threads: 2 components x T per row; at least one warp, at most 16 rows
   static constexpr int ROWS = cmax(cmax(cmin(Tune<R>::ROW_THREADS / (2 * T), 16), 1), 32 / (2 * T));
@@ -55,7 +62,7 @@ template <typename R, int N> struct RowCfg {
 };
 
 template <typename R, int N> struct ColCfg {
-  static constexpr int E = cmin(N, Tune<R>::COL_E);
+  static constexpr int E = pick_e<R>(N, Tune<R>::COL_E);
   static constexpr int T = N / E;
   static constexpr int COLS = cmax(cmin(Tune<R>::COLS, 1024 / T), 32 / T);
   static constexpr int THREADS = T * COLS;
@@ -63,7 +70,9 @@ template <typename R, int N> struct ColCfg {
   static constexpr int MINB = cmax(1, cmin(Tune<R>::COL_MINB, 1024 / THREADS));
 };
 
+// Supported line lengths: powers of two 32..4096 and 3 * 2^k for 192, 384, 768.
 inline bool size_supported(int n) {
+  if (n == 192 || n == 384 || n == 768) return true;
   return n >= 32 && n <= 4096 && (n & (n - 1)) == 0;
 }
 
@@ -73,6 +82,9 @@ template <class F> inline cudaError_t dispatch_n(int n, F&& f) {
     case 32: return f.template run<32>();
     case 64: return f.template run<64>();
     case 128: return f.template run<128>();
+    case 192: return f.template run<192>();
+    case 384: return f.template run<384>();
+    case 768: return f.template run<768>();
     case 256: return f.template run<256>();
     case 512: return f.template run<512>();
     case 1024: return f.template run<1024>();

@@ -68,7 +68,7 @@ __global__ void twiddle_kernel(sgpe::Cx<R>* out, int n, int e, int total) {
   if (i >= total) return;
   int off = 0, ns = 1;
   while (ns < n) {
-    const int rs = (n / ns < e) ? n / ns : e;
+    const int rs = sgpe::stage_radix(n, e, ns);
     const int cnt = (rs - 1) * ns;
     if (i < off + cnt) {
       const int r = (i - off) / ns + 1, k = (i - off) % ns;
@@ -169,7 +169,7 @@ extern "C" int sgpe_fft2_static(int ny, int nx, int dtype_bits, const void* in0,
                                 void* out1, int inverse, double scale, void* stream) {
   if (!in0 || !in1 || !out0 || !out1) return sgpe_detail::set_error(SGPE_ERR_ARG, "fft2_static: null data pointer");
   if (!sgpe::size_supported(nx) || !sgpe::size_supported(ny))
-    return sgpe_detail::set_error(SGPE_ERR_ARG, "fft2_static: grid sizes must be powers of two in [32, 4096]");
+    return sgpe_detail::set_error(SGPE_ERR_ARG, "fft2_static: unsupported grid size (powers of two in [32, 4096], 192, 384, 768)");
   if (dtype_bits != 64 && dtype_bits != 128)
     return sgpe_detail::set_error(SGPE_ERR_ARG, "fft2_static: dtype_bits must be 64 or 128");
   cudaStream_t s = static_cast<cudaStream_t>(stream);

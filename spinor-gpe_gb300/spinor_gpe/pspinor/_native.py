@@ -25,7 +25,8 @@ EXPORTED = ('sgpe_version', 'sgpe_last_error', 'sgpe_plan_create',
             'sgpe_plan_destroy', 'sgpe_set_physics', 'sgpe_set_substep',
             'sgpe_load_psik', 'sgpe_store_psik', 'sgpe_single_step',
             'sgpe_full_steps', 'sgpe_fft2', 'sgpe_time_passes',
-            'sgpe_fft2_static', 'sgpe_set_energy_fields', 'sgpe_energy')
+            'sgpe_fft2_static', 'sgpe_set_energy_fields', 'sgpe_energy',
+            'sgpe_batch_create', 'sgpe_batch_destroy', 'sgpe_batch_steps')
 
 
 class SgpeError(RuntimeError):
@@ -79,6 +80,10 @@ _SIGS = {
     'sgpe_set_energy_fields': ([_VP, ctypes.c_int, ctypes.POINTER(EnergyFields)],
                                ctypes.c_int),
     'sgpe_energy': ([_VP, ctypes.c_int, _VP, _VP, _VP, _VP], ctypes.c_int),
+    'sgpe_batch_create': ([ctypes.POINTER(_VP), ctypes.POINTER(_VP), ctypes.c_int],
+                          ctypes.c_int),
+    'sgpe_batch_destroy': ([_VP], ctypes.c_int),
+    'sgpe_batch_steps': ([_VP, ctypes.c_int, _VP], ctypes.c_int),
     'sgpe_fft2_static': ([ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP,
                           _VP, _VP, ctypes.c_int, ctypes.c_double, _VP],
                          ctypes.c_int),
@@ -235,3 +240,30 @@ class Plan:
         check(load().sgpe_fft2(self._h, _ptr(inp[0]), _ptr(inp[1]),
                                _ptr(out[0]), _ptr(out[1]), int(inverse),
                                float(scale), _stream(torch, inp[0].device)))
+
+
+class Batch:
+    """Owner of a native batch of plans (``sgpe_batch``)."""
+
+    def __init__(self, plans):
+        lib = load()
+        self._plans = list(plans)          # keep the plans alive
+        arr = (_VP * len(self._plans))(*[p._h for p in self._plans])
+        h = _VP()
+        check(lib.sgpe_batch_create(ctypes.byref(h), arr, len(self._plans)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, '_h', None) is not None and self._h.value:
+            load().sgpe_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:   # interpreter shutdown
+            pass
+
+    def steps(self, torch, n_steps, device):
+        check(load().sgpe_batch_steps(self._h, int(n_steps),
+                                      _stream(torch, device)))

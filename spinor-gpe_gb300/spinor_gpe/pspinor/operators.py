@@ -87,20 +87,41 @@ def _spec(values, kind, nx):
                           'full': (1, nx)}[kind])
 
 
+class Decomposition:
+    """A real FP64 field described compactly, found once and reused for
+    every operator built from the field: ``kind`` 'uniform' / 'x' / 'y'
+    with the values along that axis, 'sep' with tables a(x), b(y)
+    (split_separable), or 'full' with the field itself."""
+
+    def __init__(self, energy):
+        e = np.asarray(energy, dtype=np.float64)
+        self.shape = e.shape
+        kind, vals = _axes_profile(e)
+        if kind is not None:
+            self.kind, self.vals = kind, vals
+            return
+        sep = split_separable(e)
+        if sep is not None:
+            self.kind, self.vals = 'sep', sep
+        else:
+            self.kind, self.vals = 'full', e
+
+
+def _decomposed(energy):
+    return energy if isinstance(energy, Decomposition) else Decomposition(energy)
+
+
 def phase_op(energy, t):
-    """exp(-i E t) for a real FP64 field E as a pair of specs (a, b) whose
-    product is the operator."""
-    e = np.asarray(energy, dtype=np.float64)
-    ny, nx = e.shape
-    kind, vals = _axes_profile(e)
-    if kind is not None:
-        return _spec(np.exp(-1.0j * vals * t), kind, nx), one()
-    sep = split_separable(e)
-    if sep is not None:
-        a, b = sep
+    """exp(-i E t) for a real FP64 field E (an array or its
+    ``Decomposition``) as a pair of specs (a, b) whose product is the
+    operator."""
+    d = _decomposed(energy)
+    nx = d.shape[1]
+    if d.kind == 'sep':
+        a, b = d.vals
         return (_spec(np.exp(-1.0j * a * t), 'x', nx),
                 _spec(np.exp(-1.0j * b * t), 'y', nx))
-    return _spec(np.exp(-1.0j * e * t), 'full', nx), one()
+    return _spec(np.exp(-1.0j * d.vals * t), d.kind, nx), one()
 
 
 def value_op(values, nx):
@@ -112,25 +133,40 @@ def value_op(values, nx):
     return _spec(vals, kind, nx)
 
 
+class Compressed:
+    """A field reduced along its constant axes (``_axes_profile``), so that
+    element-wise functions are evaluated once per distinct value; ``apply``
+    returns the spec of f(field), value for value what f of the full field
+    gives."""
+
+    def __init__(self, values):
+        v = np.asarray(values)
+        self.nx = v.shape[1]
+        kind, vals = _axes_profile(v)
+        self.kind, self.vals = (kind, vals) if kind is not None else ('full', v)
+
+    def apply(self, fn):
+        out = np.asarray(fn(self.vals), dtype=np.complex128)
+        if self.kind == 'full':
+            return value_op(out, self.nx)
+        return _spec(out, self.kind, self.nx)
+
+
 def zero():
     return FieldSpec(np.zeros(1, dtype=np.complex128), 0, 0)
 
 
 def energy_pair(energy):
-    """A real FP64 energy field as two specs whose sum is the field: one
-    compressed spec and zero when it is constant along an axis, an x-table
-    plus a y-table when it is separable (a(x) + b(y) to 8 ulp), else the
-    full field and zero."""
-    e = np.asarray(energy, dtype=np.float64)
-    nx = e.shape[1]
-    kind, vals = _axes_profile(e)
-    if kind is not None:
-        return _spec(vals, kind, nx), zero()
-    sep = split_separable(e)
-    if sep is not None:
-        a, b = sep
+    """A real FP64 energy field (an array or its ``Decomposition``) as two
+    specs whose sum is the field: one compressed spec and zero when it is
+    constant along an axis, an x-table plus a y-table when it is separable
+    (a(x) + b(y) to 8 ulp), else the full field and zero."""
+    d = _decomposed(energy)
+    nx = d.shape[1]
+    if d.kind == 'sep':
+        a, b = d.vals
         return _spec(a, 'x', nx), _spec(b, 'y', nx)
-    return _spec(e, 'full', nx), zero()
+    return _spec(d.vals, d.kind, nx), zero()
 
 
 def natural_order(k_field):
@@ -138,9 +174,33 @@ def natural_order(k_field):
     return np.fft.ifftshift(np.asarray(k_field))
 
 
-def build_substep(t_sub, kin_eng_spin, pot_eng_spin, coupling, expon, outer):
+class Prepared:
+    """The sub-step inputs decomposed once for both sub-steps: kinetic
+    fields in natural order and potentials as ``Decomposition`` objects
+    (equal fields share one), coupling and Raman phase as ``Compressed``."""
+
+    def __init__(self, kin_eng_spin, pot_eng_spin, coupling, expon):
+        self.kin = self.decompose([natural_order(k) for k in kin_eng_spin])
+        self.pot = self.decompose(pot_eng_spin)
+        self.coupling = Compressed(np.asarray(coupling, dtype=np.float64))
+        self.expon = (None if expon is None else
+                      Compressed(np.asarray(expon, dtype=np.float64)))
+
+    @staticmethod
+    def decompose(fields):
+        """Decompositions of two component fields (one shared when equal)."""
+        f = [np.asarray(x, dtype=np.float64) for x in fields]
+        d0 = Decomposition(f[0])
+        if f[1] is f[0] or np.array_equal(f[1], f[0]):
+            return [d0, d0]
+        return [d0, Decomposition(f[1])]
+
+
+def build_substep(t_sub, kin_eng_spin, pot_eng_spin, coupling, expon, outer,
+                  prepared=None):
     """Operators of one sub-step of duration ``t_sub`` (complex in imaginary
-    time).
+    time).  ``prepared`` (a ``Prepared`` of the same inputs) skips the
+    decomposition of the fields.
 
     kinetic  exp(-i K_c t/2)                 (tensor_propagator.py:138, 144)
     potential exp(-i V_c t)                  (:140, 146)
@@ -149,26 +209,27 @@ def build_substep(t_sub, kin_eng_spin, pot_eng_spin, coupling, expon, outer):
                                              (:142, 148; tensor_tools.py:586-590)
     interaction exp(-i E_int t/2) = exp(z E_int), z = -i t/2  (:247-249)
     """
+    if prepared is None:
+        prepared = Prepared(kin_eng_spin, pot_eng_spin, coupling, expon)
     spec = SubstepSpec()
-    nx = np.asarray(pot_eng_spin[0]).shape[1]
     for c in range(2):
-        ka, kb = phase_op(natural_order(kin_eng_spin[c]), t_sub / 2)
+        ka, kb = phase_op(prepared.kin[c], t_sub / 2)
         spec.kin_a.append(ka)
         spec.kin_b.append(kb)
-        pa, pb = phase_op(pot_eng_spin[c], t_sub)
+        pa, pb = phase_op(prepared.pot[c], t_sub)
         spec.pot_a.append(pa)
         spec.pot_b.append(pb)
-    omega = np.asarray(coupling, dtype=np.float64)
     if outer:
-        arg = (omega / 2) * t_sub / 2
+        def arg(omega):
+            return (omega / 2) * t_sub / 2
     else:
-        arg = omega * (t_sub / 2) / 2
-    spec.cpl_c = value_op(np.cos(arg), nx)
-    spec.cpl_s = value_op(-1.0j * np.sin(arg), nx)
-    if expon is None:
+        def arg(omega):
+            return omega * (t_sub / 2) / 2
+    spec.cpl_c = prepared.coupling.apply(lambda w: np.cos(arg(w)))
+    spec.cpl_s = prepared.coupling.apply(lambda w: -1.0j * np.sin(arg(w)))
+    if prepared.expon is None:
         spec.cpl_e = one()
     else:
-        spec.cpl_e = value_op(np.exp(1.0j * np.asarray(expon, np.float64)),
-                              nx)
+        spec.cpl_e = prepared.expon.apply(lambda e: np.exp(1.0j * e))
     spec.int_z = -1.0j * t_sub / 2
     return spec

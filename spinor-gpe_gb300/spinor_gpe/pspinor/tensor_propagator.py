@@ -185,10 +185,14 @@ class TensorPropagator:
         self._plan.set_physics(float(self.g_sc['uu']), float(self.g_sc['dd']),
                                float(self.g_sc['ud']), float(self.atom_num),
                                dv_r, dv_k, self.is_coupling)
+        self._prepared = ops.Prepared(self._kin_np, self._pot_np,
+                                      self._coupling_np, self._expon_np)
         spec_out = ops.build_substep(self.dt_out, self._kin_np, self._pot_np,
-                                     self._coupling_np, self._expon_np, True)
+                                     self._coupling_np, self._expon_np, True,
+                                     self._prepared)
         spec_in = ops.build_substep(self.dt_in, self._kin_np, self._pot_np,
-                                    self._coupling_np, self._expon_np, False)
+                                    self._coupling_np, self._expon_np, False,
+                                    self._prepared)
         self._plan.set_substep(0, spec_out)
         self._plan.set_substep(1, spec_in)
         self.eng_out = SubstepOperators(self, 0, spec_out)
@@ -322,8 +326,9 @@ class TensorPropagator:
         propagated, V_c, coupling h = (Omega/2) exp(-i theta)).  Slot 1: the
         original's reporting convention (tensor_propagator.py:308-324):
         free kinetic energy plus kL kx with coupling, h = Omega/2."""
-        kin0 = [ops.energy_pair(k) for k in self._kin_np]
-        pot = [ops.energy_pair(v) for v in self._pot_np]
+        kin0 = [ops.energy_pair(d)
+                for d in ops.Prepared.decompose(self._kin_np)]
+        pot = [ops.energy_pair(d) for d in self._prepared.pot]
         theta = 0.0 if self._expon_np is None else self._expon_np
         nx = self._shape[1]
         cpl0 = ops.value_op(self._coupling_np / 2 * np.exp(-1.0j * theta), nx)
@@ -347,6 +352,21 @@ class TensorPropagator:
         out = torch.empty(10, dtype=torch.float64, device=self._device)
         self._plan.energy(torch, slot, psik, out)
         return out.cpu().numpy()
+
+    def energy_to(self, out, psik=None, slot=0):
+        """Queue the FP64 energy functional of ``psik`` (default: the current
+        state) into ``out``, a float64 device tensor of 10 values ordered as
+        ``ENERGY_KEYS``, on the current stream, without waiting for it."""
+        if psik is None:
+            psik = self.psik
+        psik = [torch.as_tensor(p, device=self._device).to(self._ctype)
+                .contiguous() for p in psik]
+        if (out.dtype != torch.float64 or out.device != self._device
+                or out.numel() != 10 or not out.is_contiguous()):
+            raise ValueError('out must be 10 contiguous float64 values on the '
+                             'propagator device')
+        self._plan.energy(torch, slot, psik, out)
+        return out
 
     def energy(self, psik=None):
         """FP64 energy functional of ``psik`` (default: the current state),

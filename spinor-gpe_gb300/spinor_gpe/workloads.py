@@ -120,3 +120,75 @@ def vortex_2048(spinor_cls, fft_2d, path, n=2048, seed=3):
     return build(spinor_cls, fft_2d, path, nx=n, ny=n, half_x=half,
                  half_y=half, g=g, lam=1.2, omega=0.5, k_l=2.0, seed=seed,
                  vortices=vort)
+
+
+def batched_uneven(spinor_cls, fft_2d, path, n_solves=96, seed=4,
+                   sizes=(128, 192, 256, 384, 512, 768, 1024)):
+    """Independent ground-state problems with seeded uneven grids and
+    parameters: side N from ``sizes`` with dx = 0.125, trap aspect
+    lam ~ U[0.5, 2], g_uu ~ U[100, 2000], g_dd = 0.995 g_uu, g_ud = 0.99 g_uu,
+    Omega ~ U[0, 2], delta ~ U[-0.5, 0.5], k_L = 3 (non-rotated frame).
+    Returns a list of PSpinor objects."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_solves):
+        n = int(rng.choice(sizes))
+        lam = float(rng.uniform(0.5, 2.0))
+        guu = float(rng.uniform(100.0, 2000.0))
+        omega = float(rng.uniform(0.0, 2.0))
+        delta = float(rng.uniform(-0.5, 0.5))
+        half = n * 0.125 / 2
+        out.append(build(spinor_cls, fft_2d, f'{path}solve{i:03d}/', nx=n, ny=n,
+                         half_x=half, half_y=half,
+                         g=(guu, 0.995 * guu, 0.99 * guu), lam=lam,
+                         omega=omega, k_l=3.0, delta=delta,
+                         rot_coupling=False, seed=seed * 1000 + i))
+    return out
+
+
+def served_stream(rate=200.0, window=60.0, seed=5, ground_frac=0.7,
+                  ground_sizes=(256, 512), quench_size=1024):
+    """Seeded request stream: Poisson arrivals at ``rate`` per second over
+    ``window`` seconds.  A fraction ``ground_frac`` are imaginary-time ground
+    states (side from ``ground_sizes``, dx = 0.125, parameters drawn as in
+    ``batched_uneven``, dt = 0.02, stop at |dE| < 1e-8 per step or 3000
+    steps); the rest are real-time quenches (side ``quench_size`` over
+    [-32, 32)^2, g = (1000, 1000, 990), Omega = 1, k_L = 3, detuning
+    0 -> U[0.1, 1], dt = 1e-3, 5000 steps) from the Thomas-Fermi start.
+    Returns request descriptions (dicts); ``request_spin`` builds one."""
+    rng = np.random.default_rng(seed)
+    out = []
+    t = 0.0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= window:
+            return out
+        rid = len(out)
+        if rng.uniform() < ground_frac:
+            n = int(rng.choice(ground_sizes))
+            guu = float(rng.uniform(100.0, 2000.0))
+            out.append({'rid': rid, 'arrival': t, 'kind': 'ground', 'n': n,
+                        'half': n * 0.125 / 2,
+                        'g': (guu, 0.995 * guu, 0.99 * guu),
+                        'lam': float(rng.uniform(0.5, 2.0)),
+                        'omega': float(rng.uniform(0.0, 2.0)),
+                        'delta': float(rng.uniform(-0.5, 0.5)),
+                        'time': 'imag', 'dt': 0.02, 'max_steps': 3000,
+                        'tol': 1e-8, 'seed': seed * 100000 + rid})
+        else:
+            n = int(quench_size)
+            out.append({'rid': rid, 'arrival': t, 'kind': 'quench', 'n': n,
+                        'half': n * 0.0625 / 2, 'g': (1000.0, 1000.0, 990.0),
+                        'lam': 1.0, 'omega': 1.0,
+                        'delta': float(rng.uniform(0.1, 1.0)),
+                        'time': 'real', 'dt': 1e-3, 'max_steps': 5000,
+                        'tol': None, 'seed': seed * 100000 + rid})
+
+
+def request_spin(spinor_cls, fft_2d, path, req):
+    """The PSpinor of one ``served_stream`` request."""
+    return build(spinor_cls, fft_2d, f"{path}req{req['rid']:06d}/",
+                 nx=req['n'], ny=req['n'], half_x=req['half'],
+                 half_y=req['half'], g=req['g'], lam=req['lam'],
+                 omega=req['omega'], k_l=3.0, delta=req['delta'],
+                 rot_coupling=False, seed=req['seed'])

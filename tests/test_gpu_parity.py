@@ -342,3 +342,65 @@ def test_eng_expect_matches_reference_convention(tp, tmp_path):
     np.testing.assert_allclose(got[2:], ref[2:], rtol=1e-11)
     assert abs(got[1] - ref[1]) / ref[1] < 0.03
     assert abs(got[0] - ref[0]) / ref[0] < 1e-3
+
+
+@pytest.mark.parametrize('shape', [(192, 192), (384, 192), (192, 768), (768, 768)])
+@pytest.mark.parametrize('dtype', [torch.complex64, torch.complex128])
+def test_fft_2d_radix3_sizes_match_numpy(shape, dtype):
+    """Grid sides 3 * 2^k (radix-3 stage) against NumPy."""
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    rng = np.random.default_rng(8)
+    a = [rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+         for _ in range(2)]
+    dr = (0.125, 0.125)
+    t = [torch.as_tensor(x, dtype=dtype, device='cuda') for x in a]
+    tol = 1e-14 if dtype == torch.complex128 else 2e-6
+    assert rel_l2([x.cpu().numpy() for x in ttools.fft_2d(t, dr)],
+                  ttools.fft_2d(a, dr)) <= tol
+    assert rel_l2([x.cpu().numpy() for x in ttools.ifft_2d(t, dr)],
+                  ttools.ifft_2d(a, dr)) <= tol
+
+
+@pytest.mark.parametrize('n,dtype', [(192, 128), (384, 64), (768, 64)])
+def test_radix3_grid_propagation_against_oracle(tp, tmp_path, n, dtype):
+    from spinor_gpe import workloads
+    from spinor_gpe.pspinor import pspinor as spin
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    ps = workloads.build(spin.PSpinor, ttools.fft_2d, str(tmp_path / 'r3') + '/',
+                         nx=n, ny=n, half_x=n * 0.0625, half_y=n * 0.0625,
+                         g=(400.0, 398.0, 396.0), lam=1.2, omega=0.8, k_l=3.0,
+                         delta=0.1, seed=21)
+    steps = 6
+    ref, ref_pops = _oracle_run(_inputs_from_spin(ps), 0.02, 'imag', steps)
+    prop = tp.TensorPropagator(ps, 0.02, steps, 'cuda', time='imag', dtype=dtype)
+    pops = torch.empty((steps, 2), dtype=torch.float64, device='cuda')
+    prop.full_steps(steps, pops)
+    got = np.array([t.cpu().numpy() for t in prop.psik])
+    assert rel_l2(got, ref) <= TOL[dtype]
+
+
+def test_batch_matches_solves_alone(tp, tmp_path):
+    """A batch of uneven solves (sizes, parameters, precision, time) advanced
+    together gives exactly what each gives when stepped alone."""
+    from spinor_gpe import workloads
+    from spinor_gpe.batch import PropagatorBatch
+    from spinor_gpe.pspinor import pspinor as spin
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    spins = workloads.batched_uneven(spin.PSpinor, ttools.fft_2d,
+                                     str(tmp_path) + '/b/', n_solves=5,
+                                     sizes=(64, 128, 192))
+    kinds = [('imag', 64), ('imag', 128), ('real', 64), ('imag', 64), ('real', 128)]
+
+    def make():
+        return [tp.TensorPropagator(s, 0.02 if t == 'imag' else 1e-3, 20, 'cuda',
+                                    time=t, dtype=d)
+                for s, (t, d) in zip(spins, kinds)]
+    alone, together = make(), make()
+    for p in alone:
+        p.full_steps(19)
+    batch = PropagatorBatch(together)
+    batch.full_steps(19)            # eager first step, then 8-, 8-, 1-, 1-step graphs
+    for a, b in zip(alone, together):
+        np.testing.assert_array_equal(np.array([t.cpu().numpy() for t in a.psik]),
+                                      np.array([t.cpu().numpy() for t in b.psik]))
+    batch.close()

@@ -76,8 +76,8 @@ def run_solver(ps, dt, n, time_mode, dtype):
     return prop, psik, n / dt_s
 
 
-def run_oracle(ps, dt, n, time_mode):
-    orc = OraclePropagator(inputs(ps), dt, time_mode, 128, device='cuda')
+def run_oracle(ps, dt, n, time_mode, dtype=128):
+    orc = OraclePropagator(inputs(ps), dt, time_mode, dtype, device='cuda')
     for _ in range(n):
         orc.full_step()
     return orc.psik_numpy()
@@ -108,27 +108,35 @@ def raman_quench_1024(tmp):
     ps = workloads.raman_quench_1024(spin.PSpinor, ttools.fft_2d, tmp + '/c2/')
     prop, mine_g, rate_i = run_solver(ps, 0.01, 3000, 'imag', 64)
     ref_g = run_oracle(ps, 0.01, 3000, 'imag')
+    ref_g64 = run_oracle(ps, 0.01, 3000, 'imag', 64)
     ground_err = rel_l2(mine_g, ref_g)
+    print(json.dumps({'config': 'raman_quench_1024 ground state (complex64, 3000 imaginary steps)',
+                      'psik_rel_l2': ground_err,
+                      'original_complex64_psik_rel_l2': rel_l2(ref_g64, ref_g)}), flush=True)
     # quench from the same (oracle) ground state for both
     ps.psik = list(ref_g)
     ps.detuning_uniform(0.5)
     e0 = oracle_energy(ps, ref_g)[4]
     prop, mine, rate = run_solver(ps, 1e-3, 10000, 'real', 64)
     ref = run_oracle(ps, 1e-3, 10000, 'real')
+    ref64 = run_oracle(ps, 1e-3, 10000, 'real', 64)
     summary('raman_quench_1024 (complex64, 3000 imag + 10000 real steps)', ps,
             mine, ref, rate,
             {'ground_state_psik_rel_l2': ground_err, 'imag_steps_per_s': rate_i,
+             'original_complex64_psik_rel_l2': rel_l2(ref64, ref),
              'energy_drift_solver': (oracle_energy(ps, mine)[4] - e0) / abs(e0),
+             'energy_drift_original_complex64': (oracle_energy(ps, ref64)[4] - e0) / abs(e0),
              'energy_drift_oracle': (oracle_energy(ps, ref)[4] - e0) / abs(e0)})
 
 
 def vortex_2048(tmp):
     ps = workloads.vortex_2048(spin.PSpinor, ttools.fft_2d, tmp + '/c3/')
     ref = run_oracle(ps, 0.01, 2000, 'imag')
+    ref64 = run_oracle(ps, 0.01, 2000, 'imag', 64)
     for dtype in (64, 128):
         _, mine, rate = run_solver(ps, 0.01, 2000, 'imag', dtype)
         summary(f'vortex_2048 (complex{dtype}, 2000 imaginary steps)', ps, mine,
-                ref, rate)
+                ref, rate, {'original_complex64_psik_rel_l2': rel_l2(ref64, ref)})
 
 
 CONFIGS = {'ground_state_256': ground_state_256,

@@ -175,9 +175,10 @@ int sgpe_time_passes(sgpe_plan* plan, int n_steps, double* col_ms, double* row_m
 
 /* A batch of plans stepped together (many independent solves, uneven grid
  * sizes and parameters).  The plans stay owned by the caller and must
- * outlive the batch; they must be on one device and not be stepped through
- * other calls while the batch exists.  No counterpart in the original
- * (which runs one solve per process). */
+ * outlive the batch and be on one device.  While the batch exists the plans
+ * may still be stepped, read and loaded on their own; when a plan's physics
+ * or operators are replaced, the batch re-captures its graphs at its next
+ * step.  No counterpart in the original (which runs one solve per process). */
 typedef struct sgpe_batch sgpe_batch;
 int sgpe_batch_create(sgpe_batch** batch, sgpe_plan* const* plans, int n_plans);
 int sgpe_batch_destroy(sgpe_batch* batch);

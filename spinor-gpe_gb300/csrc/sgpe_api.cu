@@ -128,6 +128,9 @@ struct sgpe_plan {
   cudaStream_t cap_stream = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   bool graphs_enabled = true;
+  // incremented whenever captured launches would go stale (new physics or
+  // operators); batches compare it with the value at their capture
+  unsigned long long epoch = 0;
 };
 
 namespace {
@@ -144,6 +147,7 @@ struct sgpe_batch {
   cudaEvent_t fork = nullptr;
   std::vector<cudaEvent_t> joins;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // 1 step, kGraphSteps steps
+  std::vector<unsigned long long> epoch[2];        // plans' epochs at capture
 };
 
 namespace {
@@ -383,7 +387,7 @@ template <typename R> cudaError_t col_pass_step(sgpe_plan* p, int sub, double* p
     a.k1 = kin_pair<R>(p->pair[p->prev_sub][sub]);
   }
   a.scale = R(1);
-  a.part = p->part;
+  a.part = reinterpret_cast<R*>(p->part);
   return sgpe::launch_col<R>(a, p->ny, s);
 }
 
@@ -396,7 +400,7 @@ template <typename R> cudaError_t row_pass_step(sgpe_plan* p, int sub, double* p
   a.tw = cst<R>(p->tw_x);
   a.mode = sgpe::kRowStep;
   a.scale = R(1);
-  a.part = p->part;
+  a.part = reinterpret_cast<R*>(p->part);
   a.ntile = p->ntile;
   a.norm_num = p->atom_num / (double(p->nx) * double(p->ny) * p->dv_r);
   a.g_uu = R(p->g[0]);
@@ -449,14 +453,14 @@ template <typename R> int store(sgpe_plan* p, void* o0, void* o1, double* pops, 
   a.nk = 1;
   a.k1 = kin_op<R>(p->sub[p->prev_sub]);
   a.scale = R(1);
-  a.part = p->part;
+  a.part = reinterpret_cast<R*>(p->part);
   cudaError_t e = sgpe::launch_col<R>(a, p->ny, s);
   if (e != cudaSuccess) return cuda_fail(e, "store (column pass)");
   sgpe::ScaleArgs<R> sa{};
   sa.d[0] = st<R>(o0);
   sa.d[1] = st<R>(o1);
   sa.n = (long long)p->nx * p->ny;
-  sa.part = p->part;
+  sa.part = reinterpret_cast<const R*>(p->part);
   sa.ntile = p->ntile;
   sa.atom_num = p->atom_num;
   sa.dv = p->dv_k;
@@ -575,6 +579,7 @@ int energy_impl(sgpe_plan* p, int slot, const void* k0, const void* k1, double* 
 }
 
 void drop_graphs(sgpe_plan* p) {
+  ++p->epoch;
   for (auto& g : p->graph) {
     if (g) cudaGraphExecDestroy(g);
     g = nullptr;
@@ -1030,7 +1035,20 @@ int capture_batch(sgpe_batch* b, int steps, cudaGraphExec_t* out) {
   }
   e = cudaGraphInstantiate(out, graph, 0);
   cudaGraphDestroy(graph);
-  return e == cudaSuccess ? SGPE_OK : cuda_fail(e, "batch graph instantiate");
+  if (e != cudaSuccess) return cuda_fail(e, "batch graph instantiate");
+  std::vector<unsigned long long>& ep = b->epoch[steps == 1 ? 0 : 1];
+  ep.clear();
+  for (sgpe_plan* p : b->plans) ep.push_back(p->epoch);
+  return SGPE_OK;
+}
+
+// True when some plan's physics or operators changed since graph k was
+// captured.
+bool batch_stale(const sgpe_batch* b, int k) {
+  if (b->epoch[k].size() != b->plans.size()) return true;
+  for (size_t i = 0; i < b->plans.size(); ++i)
+    if (b->plans[i]->epoch != b->epoch[k][i]) return true;
+  return false;
 }
 }  // namespace
 
@@ -1057,6 +1075,10 @@ int sgpe_batch_steps(sgpe_batch* b, int n_steps, void* stream) {
   }
   while (done < n_steps) {
     const int k = (n_steps - done >= kGraphSteps) ? 1 : 0;
+    if (b->graph[k] != nullptr && batch_stale(b, k)) {
+      cudaGraphExecDestroy(b->graph[k]);
+      b->graph[k] = nullptr;
+    }
     if (b->graph[k] == nullptr) {
       const int rc = capture_batch(b, k ? kGraphSteps : 1, &b->graph[k]);
       if (rc != SGPE_OK) return rc;

@@ -141,7 +141,7 @@ template <typename R> struct RowArgs {
   R scale;                // forward/inverse modes: constant output scale
   // step mode: renormalisation from the partial sums of the preceding
   // column pass, lambda = sqrt(norm_num / sum w)
-  const double* part;     // [2 comps][ntile][u, w]
+  const R* part;          // [2 comps][ntile][u, w]
   int ntile;
   double norm_num;        // atom_num / (Nx Ny dv_r)
   R g_uu, g_dd, g_ud;
@@ -163,14 +163,15 @@ template <typename R> struct ColArgs {
   KinOp<R> k1, k2;        // k1 first; u = sum|psik|^2 after k1, w after k2
                           // (w = u when nk < 2)
   R scale;
-  double* part;           // non-null: per-block partial sums [comp][tile][u, w]
-                          // (FP64; the consumer of the pass sums them)
+  R* part;                // non-null: per-block partial sums [comp][tile][u, w]
+                          // in the working precision; the consumer of the
+                          // pass sums them with (at least) FP64 accuracy
 };
 
 template <typename R> struct ScaleArgs {
   Cx<R>* d[2];
   long long n;            // elements per component
-  const double* part;     // partials of the column pass that wrote d
+  const R* part;          // partials of the column pass that wrote d
   int ntile;
   double atom_num, dv;
   double* pops;
@@ -191,8 +192,9 @@ template <typename T> __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-// Sums of the column-pass partials [2][ntile][u, w] by one warp, in FP64 and
-// a fixed order: (sum u_0, sum u_1, sum w) returned on every lane.
+// Sums of the column-pass partials [2][ntile][u, w] by one warp, in a fixed
+// order: (sum u_0, sum u_1, sum w) returned on every lane.
+// FP64 partials are summed in FP64.
 __device__ __forceinline__ void sum_partials(const double* part, int ntile, int lane, double* u0, double* u1,
                                              double* w) {
   double su0 = 0.0, su1 = 0.0, sw = 0.0;
@@ -204,6 +206,86 @@ __device__ __forceinline__ void sum_partials(const double* part, int ntile, int 
   *u0 = warp_sum(su0);
   *u1 = warp_sum(su1);
   *w = warp_sum(sw);
+}
+
+// Double-float accumulator: the value is hi + lo with |lo| <= ulp(hi)/2, so
+// sums of FP32 terms keep about 48 significant bits using FP32 arithmetic
+// only (Knuth's TwoSum for each addition; Dekker's FastTwoSum to
+// renormalise).  FP64 arithmetic runs at a small fraction of the FP32 rate on
+// this GPU, which made the FP64 sum of the partials a serial bottleneck at
+// the start of every row-pass block.
+struct FloatFloat {
+  float hi = 0.0f, lo = 0.0f;
+  __device__ __forceinline__ void add(float x) {
+    const float s = hi + x;
+    const float bp = s - hi;
+    const float err = (hi - (s - bp)) + (x - bp);
+    hi = s;
+    lo += err;
+  }
+  __device__ __forceinline__ void add(const FloatFloat& o) {
+    const float s = hi + o.hi;
+    const float bp = s - hi;
+    float err = (hi - (s - bp)) + (o.hi - bp);
+    err += lo + o.lo;
+    hi = s + err;                 // FastTwoSum(s, err), |s| >= |err|
+    lo = err - (hi - s);
+  }
+  __device__ __forceinline__ void warp_reduce() {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      FloatFloat t;
+      t.hi = __shfl_xor_sync(0xffffffffu, hi, o);
+      t.lo = __shfl_xor_sync(0xffffffffu, lo, o);
+      add(t);
+    }
+  }
+  __device__ __forceinline__ double value() const { return double(hi) + double(lo); }
+};
+
+// FP32 partials: double-float sums in FP32 arithmetic.  Every lane of the
+// warp ends with the same bits (the butterfly adds the same pairs in the same
+// order on all lanes up to commutation, and each step is commutative).
+__device__ __forceinline__ void sum_partials(const float* part, int ntile, int lane, FloatFloat* u0,
+                                             FloatFloat* u1, FloatFloat* w) {
+  FloatFloat su0, su1, sw;
+  for (int i = lane; i < 2 * ntile; i += 32) {
+    const float2 uw = reinterpret_cast<const float2*>(part)[i];
+    sw.add(uw.y);
+    if (i < ntile) su0.add(uw.x); else su1.add(uw.x);
+  }
+  su0.warp_reduce();
+  su1.warp_reduce();
+  sw.warp_reduce();
+  *u0 = su0;
+  *u1 = su1;
+  *w = sw;
+}
+__device__ __forceinline__ void sum_partials(const float* part, int ntile, int lane, double* u0, double* u1,
+                                             double* w) {
+  FloatFloat a, b, c;
+  sum_partials(part, ntile, lane, &a, &b, &c);
+  *u0 = a.value();
+  *u1 = b.value();
+  *w = c.value();
+}
+
+// lambda = sqrt(num / w) of the row pass, in the working precision.
+__device__ __forceinline__ float row_lambda(const float* part, int ntile, int lane, float norm_num, double* u0,
+                                            double* u1, bool want_u) {
+  FloatFloat a, b, c;
+  sum_partials(part, ntile, lane, &a, &b, &c);
+  if (want_u) {
+    *u0 = a.value();
+    *u1 = b.value();
+  }
+  return sqrtf(norm_num / (c.hi + c.lo));
+}
+__device__ __forceinline__ double row_lambda(const double* part, int ntile, int lane, double norm_num, double* u0,
+                                             double* u1, bool) {
+  double sw;
+  sum_partials(part, ntile, lane, u0, u1, &sw);
+  return sqrt(norm_num / sw);
 }
 
 // Sum of |v[m]|^2 over the E points of a thread, pairwise in the working
@@ -337,7 +419,7 @@ row_kernel(const RowArgs<R> a) {
   constexpr int NT = 2 * T * ROWS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* sm = reinterpret_cast<C*>(smem_raw);
-  __shared__ double s_lambda;
+  __shared__ R s_lambda;
 
   const int tid = threadIdx.x;
   const int rho = tid / (2 * T);
@@ -362,18 +444,19 @@ row_kernel(const RowArgs<R> a) {
     // warp 0 does this after its own part of the transform, so the other
     // warps are not held up
     if (tid < 32) {
-      double su0, su1, sw;
-      sum_partials(a.part, a.ntile, tid, &su0, &su1, &sw);
+      double su0 = 0.0, su1 = 0.0;
+      const bool want_u = (a.pops != nullptr && blockIdx.x == 0);
+      const R l = row_lambda(a.part, a.ntile, tid, R(a.norm_num), &su0, &su1, want_u);
       if (tid == 0) {
-        s_lambda = sqrt(a.norm_num / sw);
-        if (a.pops != nullptr && blockIdx.x == 0) {
+        s_lambda = l;
+        if (want_u) {
           a.pops[0] = a.atom_num * su0 / (su0 + su1);
           a.pops[1] = a.atom_num * su1 / (su0 + su1);
         }
       }
     }
     __syncthreads();
-    const R lam = R(s_lambda);
+    const R lam = s_lambda;
     // point-wise operators: the 2T threads of a row share its N points
     {
       const LineSmem<C, E> r0{sm + rho * LS, 0};
@@ -474,9 +557,9 @@ col_kernel(const ColArgs<R> a) {
       bu = warp_sum(bu);
       bw = warp_sum(bw);
       if (lane == 0) {
-        double* dst = a.part + 2 * ((long long)comp * gridDim.x + blockIdx.x);
-        dst[0] = double(bu);
-        dst[1] = double(bw);
+        R* dst = a.part + 2 * ((long long)comp * gridDim.x + blockIdx.x);
+        dst[0] = bu;
+        dst[1] = bw;
       }
     }
   }

@@ -33,22 +33,35 @@ template <typename R> struct Tune;
 #ifndef SGPE_F32_COL_MINB
 #define SGPE_F32_COL_MINB 2
 #endif
+// Sides 3 * 2^k: points per thread (a multiple of 3, so that the radix-3
+// stage divides it) and the register caps of their passes.
+#ifndef SGPE_F32_R3_E
+#define SGPE_F32_R3_E 12
+#endif
+#ifndef SGPE_F32_R3_ROW_MINB
+#define SGPE_F32_R3_ROW_MINB 4
+#endif
+#ifndef SGPE_F32_R3_COL_MINB
+#define SGPE_F32_R3_COL_MINB 4
+#endif
 template <> struct Tune<float> {
   static constexpr int ROW_E = SGPE_F32_ROW_E, ROW_THREADS = SGPE_F32_ROW_THREADS, ROW_MINB = SGPE_F32_ROW_MINB;
   static constexpr int COL_E = SGPE_F32_COL_E, COLS = SGPE_F32_COLS, COL_MINB = SGPE_F32_COL_MINB;
+  static constexpr int R3_E = SGPE_F32_R3_E, R3_ROW_MINB = SGPE_F32_R3_ROW_MINB, R3_COL_MINB = SGPE_F32_R3_COL_MINB;
 };
 template <> struct Tune<double> {
   static constexpr int ROW_E = 8, ROW_THREADS = 256, ROW_MINB = 2;
   static constexpr int COL_E = 8, COLS = 4, COL_MINB = 1;
+  static constexpr int R3_E = 12, R3_ROW_MINB = 2, R3_COL_MINB = 1;
 };
 
 constexpr int cmin(int a, int b) { return a < b ? a : b; }
 constexpr int cmax(int a, int b) { return a > b ? a : b; }
 
-// Points per thread: the tuned E for powers of two; 24 (complex64) or 12
-// (complex128) for N = 3 * 2^k, so that every stage radix divides it.
+// Points per thread: the tuned E for powers of two; Tune::R3_E for
+// N = 3 * 2^k, so that every stage radix divides it.
 template <typename R> constexpr int pick_e(int n, int e_pow2) {
-  return (n % 3 == 0) ? (sizeof(R) == 4 ? 24 : 12) : cmin(n, e_pow2);
+  return (n % 3 == 0) ? Tune<R>::R3_E : cmin(n, e_pow2);
 }
 
 template <typename R, int N> struct RowCfg {
@@ -58,7 +71,8 @@ template <typename R, int N> struct RowCfg {
   static constexpr int ROWS = cmax(cmax(cmin(Tune<R>::ROW_THREADS / (2 * T), 16), 1), 32 / (2 * T));
   static constexpr int THREADS = 2 * T * ROWS;
   static constexpr size_t SMEM = 2ull * ROWS * (N + N / E) * sizeof(Cx<R>);
-  static constexpr int MINB = cmax(1, cmin(Tune<R>::ROW_MINB, 1024 / THREADS));
+  static constexpr int MINB =
+      cmax(1, cmin(N % 3 == 0 ? Tune<R>::R3_ROW_MINB : Tune<R>::ROW_MINB, 1024 / THREADS));
 };
 
 template <typename R, int N> struct ColCfg {
@@ -67,7 +81,8 @@ template <typename R, int N> struct ColCfg {
   static constexpr int COLS = cmax(cmin(Tune<R>::COLS, 1024 / T), 32 / T);
   static constexpr int THREADS = T * COLS;
   static constexpr size_t SMEM = size_t(COLS) * (N + N / E + 2) * sizeof(Cx<R>);
-  static constexpr int MINB = cmax(1, cmin(Tune<R>::COL_MINB, 1024 / THREADS));
+  static constexpr int MINB =
+      cmax(1, cmin(N % 3 == 0 ? Tune<R>::R3_COL_MINB : Tune<R>::COL_MINB, 1024 / THREADS));
 };
 
 // Supported line lengths: powers of two 32..4096 and 3 * 2^k for 192, 384, 768.

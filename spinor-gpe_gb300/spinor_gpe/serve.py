@@ -284,6 +284,8 @@ def run_sequential(requests, device='cuda'):
     and the same stopping rules, on the current stream.  Returns the results
     and the device time of the stepping (set-up excluded), in seconds."""
     device = torch.device(device)
+    if device.index is None:
+        device = torch.device('cuda', torch.cuda.current_device())
     torch.cuda.set_device(device)
     stream = torch.cuda.current_stream(device)
     total = 0.0

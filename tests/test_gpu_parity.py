@@ -400,7 +400,21 @@ def test_batch_matches_solves_alone(tp, tmp_path):
         p.full_steps(19)
     batch = PropagatorBatch(together)
     batch.full_steps(19)            # eager first step, then 8-, 8-, 1-, 1-step graphs
-    for a, b in zip(alone, together):
-        np.testing.assert_array_equal(np.array([t.cpu().numpy() for t in a.psik]),
-                                      np.array([t.cpu().numpy() for t in b.psik]))
+
+    def same():
+        for a, b in zip(alone, together):
+            np.testing.assert_array_equal(
+                np.array([t.cpu().numpy() for t in a.psik]),
+                np.array([t.cpu().numpy() for t in b.psik]))
+    same()
+    # new physics for one solve: the batch re-captures its graphs
+    for p in (alone[1], together[1]):
+        g = p.g_sc
+        p._plan.set_physics(1.1 * g['uu'], 1.1 * g['dd'], 1.1 * g['ud'],
+                            float(p.atom_num), float(p._space_np['dv_r']),
+                            float(p._space_np['dv_k']), p.is_coupling)
+    for p in alone:
+        p.full_steps(9)
+    batch.full_steps(9)
+    same()
     batch.close()

@@ -45,9 +45,25 @@ struct HostField {
   int sx = 0, sy = 0;
 };
 
+// Separable form of a sub-step's operators, used by the kernels' fast
+// paths: every factor as a full-length 1-D table (x-tables of nx values,
+// y-tables of ny values; uniform values expanded), so the kernels index them
+// with compile-time strides.  Built when the fields allow it:
+//  kinetic  exp(-i K_c t/2) = kx_c(x) ky_c(ky),
+//  potential exp(-i V_c t) = px_c(x) py_c(y),
+//  coupling  c uniform, s conj(e) and s e x-tables.
+struct SepOps {
+  DevField kx[2], ky[2];
+  bool kin = false;
+  DevField px[2], py[2], s01x, s10x;
+  bool pot = false, cpl = false;
+};
+
 struct SubOps {
   DevField kin_a[2], kin_b[2], pot_a[2], pot_b[2], cc, cs, ce, s01, s10;
   bool has_s01 = false;
+  HostField s01_host, s10_host;  // FP64 off-diagonals when has_s01
+  SepOps sep;
   HostField kin_host[2][2];  // [comp][a, b]
   double zr = 0.0, zi = 0.0;
   std::vector<void*> allocs;
@@ -66,6 +82,7 @@ struct EnergyFields {
 // in the column kernel instead of two.
 struct PairOps {
   DevField a[2], b[2];
+  SepOps sep;             // kinetic part only
   std::vector<void*> allocs;
   bool set = false;
 };
@@ -266,6 +283,56 @@ HostField multiply_fields(const HostField& fa, const HostField& fb, int nx, int 
   return r;
 }
 
+// The values of a field that does not vary along y as an x-table of nx
+// values (axis 0), or along x as a y-table of ny values (axis 1); false when
+// the field varies along the other axis.
+bool expand_1d(const HostField& f, int axis, int nx, int ny, HostField* out) {
+  if (axis == 0 ? f.sy != 0 : f.sx != 0) return false;
+  const int n = axis == 0 ? nx : ny, stride = axis == 0 ? f.sx : f.sy;
+  out->sx = axis == 0 ? 1 : 0;
+  out->sy = axis == 0 ? 0 : 1;
+  out->v.assign(2 * (size_t)n, 0.0);
+  for (int i = 0; i < n; ++i) {
+    const long long k = (long long)i * stride;
+    out->v[2 * i] = f.v[2 * k];
+    out->v[2 * i + 1] = f.v[2 * k + 1];
+  }
+  return true;
+}
+
+// A product of two broadcast factors fa * fb as (x-table, y-table) when one
+// factor does not vary along y and the other not along x (either order).
+// The kernels multiply the two tables in the order (x, y); complex products
+// are commutative bit for bit (cmul uses fma(a.x, b.x, -a.y b.y) and
+// fma(a.x, b.y, a.y b.x)), so the result equals the product fa * fb.
+bool split_xy(const HostField& fa, const HostField& fb, int nx, int ny, HostField* x, HostField* y) {
+  if (expand_1d(fa, 0, nx, ny, x) && expand_1d(fb, 1, nx, ny, y)) return true;
+  return expand_1d(fb, 0, nx, ny, x) && expand_1d(fa, 1, nx, ny, y);
+}
+
+HostField host_field(const sgpe_field& f) {
+  HostField h;
+  h.v.assign(f.data, f.data + 2 * (size_t)f.n);
+  h.sx = f.sx;
+  h.sy = f.sy;
+  return h;
+}
+
+// Kinetic part of SepOps from the FP64 factors of each component.
+int build_sep_kin(sgpe_plan* p, const HostField (&a)[2], const HostField (&b)[2], SepOps* so,
+                  std::vector<void*>* allocs) {
+  HostField x[2], y[2];
+  for (int c = 0; c < 2; ++c)
+    if (!split_xy(a[c], b[c], p->nx, p->ny, &x[c], &y[c])) return SGPE_OK;  // not separable: generic path
+  for (int c = 0; c < 2; ++c) {
+    int rc = upload_host_field(p, x[c], &so->kx[c], allocs);
+    if (rc == SGPE_OK) rc = upload_host_field(p, y[c], &so->ky[c], allocs);
+    if (rc != SGPE_OK) return rc;
+  }
+  so->kin = true;
+  return SGPE_OK;
+}
+
 constexpr int kEnergyBlocks = 304;
 
 // FP64 upload of a field (energy fields keep double precision).
@@ -304,15 +371,21 @@ void free_pair(PairOps& po) {
 int ensure_pair(sgpe_plan* p, int prev, int next) {
   PairOps& po = p->pair[prev][next];
   if (po.set) return SGPE_OK;
+  HostField ma[2], mb[2];
   for (int c = 0; c < 2; ++c) {
-    const HostField ma = multiply_fields(p->sub[prev].kin_host[c][0], p->sub[next].kin_host[c][0], p->nx, p->ny);
-    const HostField mb = multiply_fields(p->sub[prev].kin_host[c][1], p->sub[next].kin_host[c][1], p->nx, p->ny);
-    int rc = upload_host_field(p, ma, &po.a[c], &po.allocs);
-    if (rc == SGPE_OK) rc = upload_host_field(p, mb, &po.b[c], &po.allocs);
+    ma[c] = multiply_fields(p->sub[prev].kin_host[c][0], p->sub[next].kin_host[c][0], p->nx, p->ny);
+    mb[c] = multiply_fields(p->sub[prev].kin_host[c][1], p->sub[next].kin_host[c][1], p->nx, p->ny);
+    int rc = upload_host_field(p, ma[c], &po.a[c], &po.allocs);
+    if (rc == SGPE_OK) rc = upload_host_field(p, mb[c], &po.b[c], &po.allocs);
     if (rc != SGPE_OK) {
       free_pair(po);
       return rc;
     }
+  }
+  const int rc = build_sep_kin(p, ma, mb, &po.sep, &po.allocs);
+  if (rc != SGPE_OK) {
+    free_pair(po);
+    return rc;
   }
   po.set = true;
   return SGPE_OK;
@@ -322,36 +395,34 @@ template <typename R> sgpe::Field<R> typed(const DevField& f) {
   return sgpe::Field<R>{static_cast<const sgpe::Cx<R>*>(f.p), f.sx, f.sy};
 }
 
-template <typename R> sgpe::KinOp<R> kin_op(const SubOps& so) {
+template <typename R> sgpe::KinOp<R> kin_from(const DevField (&a)[2], const DevField (&b)[2], const SepOps& sep) {
   sgpe::KinOp<R> k;
   for (int c = 0; c < 2; ++c) {
-    k.a[c] = typed<R>(so.kin_a[c]);
-    k.b[c] = typed<R>(so.kin_b[c]);
+    k.a[c] = typed<R>(sep.kin ? sep.kx[c] : a[c]);
+    k.b[c] = typed<R>(sep.kin ? sep.ky[c] : b[c]);
   }
+  k.sep = sep.kin ? 1 : 0;
   return k;
 }
 
-template <typename R> sgpe::KinOp<R> kin_pair(const PairOps& po) {
-  sgpe::KinOp<R> k;
-  for (int c = 0; c < 2; ++c) {
-    k.a[c] = typed<R>(po.a[c]);
-    k.b[c] = typed<R>(po.b[c]);
-  }
-  return k;
-}
+template <typename R> sgpe::KinOp<R> kin_op(const SubOps& so) { return kin_from<R>(so.kin_a, so.kin_b, so.sep); }
 
-template <typename R> sgpe::RealOp<R> real_op(const SubOps& so) {
+template <typename R> sgpe::KinOp<R> kin_pair(const PairOps& po) { return kin_from<R>(po.a, po.b, po.sep); }
+
+template <typename R> sgpe::RealOp<R> real_op(const SubOps& so, int coupling) {
   sgpe::RealOp<R> o;
+  const bool sep = so.sep.pot && (!coupling || so.sep.cpl);
   for (int c = 0; c < 2; ++c) {
-    o.pa[c] = typed<R>(so.pot_a[c]);
-    o.pb[c] = typed<R>(so.pot_b[c]);
+    o.pa[c] = typed<R>(sep ? so.sep.px[c] : so.pot_a[c]);
+    o.pb[c] = typed<R>(sep ? so.sep.py[c] : so.pot_b[c]);
   }
   o.cc = typed<R>(so.cc);
   o.cs = typed<R>(so.cs);
   o.ce = typed<R>(so.ce);
   o.has_s01 = so.has_s01 ? 1 : 0;
-  o.s01 = typed<R>(so.has_s01 ? so.s01 : so.cs);
-  o.s10 = typed<R>(so.has_s01 ? so.s10 : so.cs);
+  o.s01 = typed<R>(sep && coupling ? so.sep.s01x : so.has_s01 ? so.s01 : so.cs);
+  o.s10 = typed<R>(sep && coupling ? so.sep.s10x : so.has_s01 ? so.s10 : so.cs);
+  o.sep = sep ? 1 : 0;
   o.zr = R(so.zr);
   o.zi = R(so.zi);
   return o;
@@ -407,7 +478,7 @@ template <typename R> cudaError_t row_pass_step(sgpe_plan* p, int sub, double* p
   a.g_dd = R(p->g[1]);
   a.g_ud = R(p->g[2]);
   a.coupling = p->coupling;
-  a.op = real_op<R>(p->sub[sub]);
+  a.op = real_op<R>(p->sub[sub], p->coupling);
   a.pops = pops;
   a.atom_num = p->atom_num;
   return sgpe::launch_row<R>(a, p->nx, p->ny, s);
@@ -771,6 +842,8 @@ int sgpe_set_substep(sgpe_plan* p, int sub, const sgpe_substep_ops* ops) {
       rc = upload_host_field(p, m01, &so.s01, &so.allocs);
       if (rc == SGPE_OK) rc = upload_host_field(p, m10, &so.s10, &so.allocs);
       so.has_s01 = (rc == SGPE_OK);
+      so.s01_host = m01;
+      so.s10_host = m10;
     }
   }
   if (rc != SGPE_OK) {
@@ -783,6 +856,33 @@ int sgpe_set_substep(sgpe_plan* p, int sub, const sgpe_substep_ops* ops) {
       so.kin_host[c][k].v.assign(src[k]->data, src[k]->data + 2 * (size_t)src[k]->n);
       so.kin_host[c][k].sx = src[k]->sx;
       so.kin_host[c][k].sy = src[k]->sy;
+    }
+  }
+  // separable fast-path tables
+  {
+    const HostField ka[2] = {so.kin_host[0][0], so.kin_host[1][0]};
+    const HostField kb[2] = {so.kin_host[0][1], so.kin_host[1][1]};
+    rc = build_sep_kin(p, ka, kb, &so.sep, &so.allocs);
+    HostField px[2], py[2];
+    bool pot = (rc == SGPE_OK);
+    for (int c = 0; c < 2 && pot; ++c)
+      pot = split_xy(host_field(ops->pot_a[c]), host_field(ops->pot_b[c]), p->nx, p->ny, &px[c], &py[c]);
+    for (int c = 0; c < 2 && pot && rc == SGPE_OK; ++c) {
+      rc = upload_host_field(p, px[c], &so.sep.px[c], &so.allocs);
+      if (rc == SGPE_OK) rc = upload_host_field(p, py[c], &so.sep.py[c], &so.allocs);
+    }
+    so.sep.pot = pot && rc == SGPE_OK;
+    HostField s01x, s10x;
+    const bool cc_uniform = ops->cpl_c.sx == 0 && ops->cpl_c.sy == 0;
+    if (rc == SGPE_OK && cc_uniform && so.has_s01 && expand_1d(so.s01_host, 0, p->nx, p->ny, &s01x) &&
+        expand_1d(so.s10_host, 0, p->nx, p->ny, &s10x)) {
+      rc = upload_host_field(p, s01x, &so.sep.s01x, &so.allocs);
+      if (rc == SGPE_OK) rc = upload_host_field(p, s10x, &so.sep.s10x, &so.allocs);
+      so.sep.cpl = (rc == SGPE_OK);
+    }
+    if (rc != SGPE_OK) {
+      free_sub(so);
+      return rc;
     }
   }
   so.zr = ops->int_z_re;

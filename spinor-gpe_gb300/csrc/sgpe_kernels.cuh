@@ -54,6 +54,27 @@ __device__ __forceinline__ void allow_next_grid() {
 #endif
 }
 
+// State loads and stores of the pass kernels.  With SGPE_STATE_CG the state
+// bypasses L1 (cached in L2 only), leaving L1 to the operator and twiddle
+// tables that every block re-reads.
+#ifndef SGPE_STATE_CG
+#define SGPE_STATE_CG 0
+#endif
+template <class C> __device__ __forceinline__ C ld_state(const C* p) {
+#if SGPE_STATE_CG
+  return __ldcg(p);
+#else
+  return *p;
+#endif
+}
+template <class C> __device__ __forceinline__ void st_state(C* p, C v) {
+#if SGPE_STATE_CG
+  __stcg(p, v);
+#else
+  *p = v;
+#endif
+}
+
 // A complex operator field with broadcast strides: value(x, y) = p[x*sx + y*sy].
 // sx = sy = 0 is a uniform value, (1, 0) an x-table, (0, 1) a y-table and
 // (1, Nx) a full field.
@@ -66,8 +87,11 @@ template <typename R> __device__ __forceinline__ Cx<R> fld(const Field<R>& f, in
 }
 
 // Kinetic propagator exp(-i K_c t/2) = a_c(x, y) * b_c(x, y) in natural k order.
+// sep: a_c is an x-table of Nx values and b_c a y-table of Ny values (unit
+// strides), read with compile-time offsets.
 template <typename R> struct KinOp {
   Field<R> a[2], b[2];
+  int sep;
 };
 
 // Real-space operators of one sub-step:
@@ -82,6 +106,9 @@ template <typename R> struct RealOp {
   // on the host when that keeps them 1-D tables (has_s01), else computed here
   Field<R> s01, s10;
   int has_s01;
+  // sep: pa_c, s01, s10 are x-tables of Nx values, pb_c y-tables of Ny
+  // values (unit strides), cc is uniform
+  int sep;
   R zr, zi;
 };
 
@@ -344,12 +371,17 @@ template <typename R> __device__ __forceinline__ Cx<R> cexp_z(R zr, R zi, R e) {
   return cmake<C>(g * cs, g * sn);
 }
 
+// Operator values at one point: coupling c, s conj(e), s e; potential
+// factors (x part, y part) of each component.
+template <typename R> struct PointOps {
+  Cx<R> cc, s01, s10, pa0, pb0, pa1, pb1;
+};
+
 // Real-space operators of one sub-step at one point x of a row, both
 // components (tensor_propagator.py:247-267): interaction, coupling,
 // potential, coupling, and the interaction again with the same operator.
 template <typename R>
-__device__ __forceinline__ void real_space_ops(Cx<R>& p0, Cx<R>& p1, int x, const RowFields<R>& rf,
-                                               const RowArgs<R>& a) {
+__device__ __forceinline__ void apply_real_ops(Cx<R>& p0, Cx<R>& p1, const PointOps<R>& v, const RowArgs<R>& a) {
   using C = Cx<R>;
   const RealOp<R>& op = a.op;
   const R n0 = cabs2(p0), n1 = cabs2(p1);
@@ -359,24 +391,15 @@ __device__ __forceinline__ void real_space_ops(Cx<R>& p0, Cx<R>& p1, int x, cons
   const C i1 = cexp_z(op.zr, op.zi, e1);
   p0 = cmul(p0, i0);
   p1 = cmul(p1, i1);
-  C cc, s01, s10;
+  const C cc = v.cc, s01 = v.s01, s10 = v.s10;
   if (a.coupling) {
-    cc = rf.at(kCc, x);
-    if (op.has_s01) {
-      s01 = rf.at(kS01, x);
-      s10 = rf.at(kS10, x);
-    } else {
-      const C sv = rf.at(kCs, x), e = rf.at(kCe, x);
-      s01 = cmulc(sv, e);
-      s10 = cmul(sv, e);
-    }
     const C q0 = cadd(cmul(cc, p0), cmul(s01, p1));
     const C q1 = cadd(cmul(s10, p0), cmul(cc, p1));
     p0 = q0;
     p1 = q1;
   }
-  p0 = cmul(p0, cmul(rf.at(kPa0, x), rf.at(kPb0, x)));
-  p1 = cmul(p1, cmul(rf.at(kPa1, x), rf.at(kPb1, x)));
+  p0 = cmul(p0, cmul(v.pa0, v.pb0));
+  p1 = cmul(p1, cmul(v.pa1, v.pb1));
   if (a.coupling) {
     const C q0 = cadd(cmul(cc, p0), cmul(s01, p1));
     const C q1 = cadd(cmul(s10, p0), cmul(cc, p1));
@@ -387,11 +410,45 @@ __device__ __forceinline__ void real_space_ops(Cx<R>& p0, Cx<R>& p1, int x, cons
   p1 = cmul(p1, i1);
 }
 
+// The same with the operator values read through the generic broadcast
+// fields (any stride pattern, row-constant values hoisted by RowFields).
+template <typename R>
+__device__ __forceinline__ void real_space_ops(Cx<R>& p0, Cx<R>& p1, int x, const RowFields<R>& rf,
+                                               const RowArgs<R>& a) {
+  using C = Cx<R>;
+  PointOps<R> v;
+  if (a.coupling) {
+    v.cc = rf.at(kCc, x);
+    if (a.op.has_s01) {
+      v.s01 = rf.at(kS01, x);
+      v.s10 = rf.at(kS10, x);
+    } else {
+      const C sv = rf.at(kCs, x), e = rf.at(kCe, x);
+      v.s01 = cmulc(sv, e);
+      v.s10 = cmul(sv, e);
+    }
+  } else {
+    v.cc = v.s01 = v.s10 = C{};
+  }
+  v.pa0 = rf.at(kPa0, x);
+  v.pb0 = rf.at(kPb0, x);
+  v.pa1 = rf.at(kPa1, x);
+  v.pb1 = rf.at(kPb1, x);
+  apply_real_ops(p0, p1, v, a);
+}
+
 // v[m] *= ka(x, ky) * kb(x, ky) for ky = j + m*T along one column x; a
 // factor that does not vary along the column (sy == 0) is loaded once.
 template <typename R, int E, int T>
 __device__ __forceinline__ void apply_kinetic(Cx<R> (&v)[E], const KinOp<R>& k, int comp, int x, int j) {
   using C = Cx<R>;
+  if (k.sep) {  // x-table times y-table, unit strides
+    const C ka = __ldg(k.a[comp].p + x);
+    const C* kb = k.b[comp].p + j;
+#pragma unroll
+    for (int m = 0; m < E; ++m) v[m] = cmul(v[m], cmul(ka, __ldg(kb + m * T)));
+    return;
+  }
   const Field<R>& fa = k.a[comp];
   const Field<R>& fb = k.b[comp];
   const bool a_const = (fa.sy == 0), b_const = (fb.sy == 0);
@@ -432,7 +489,7 @@ row_kernel(const RowArgs<R> a) {
   const C* __restrict__ in = a.in[comp];
   wait_for_previous_grid();
 #pragma unroll
-  for (int m = 0; m < E; ++m) v[0][m] = in[row_off + j + m * T];
+  for (int m = 0; m < E; ++m) v[0][m] = ld_state(in + row_off + j + m * T);
   allow_next_grid();
   // line (comp, rho) at sm + (comp*ROWS + rho)*LS
   const LineSmem<C, E> smv{sm + (comp * ROWS + rho) * LS, 0};
@@ -461,16 +518,43 @@ row_kernel(const RowArgs<R> a) {
     {
       const LineSmem<C, E> r0{sm + rho * LS, 0};
       const LineSmem<C, E> r1{sm + (ROWS + rho) * LS, 0};
-      RowFields<R> rf;
-      rf.init(a.op, y);
       const int jj = tid % (2 * T);
+      if (a.op.sep) {
+        // separable operators: x-tables read at jj + m*2T (compile-time
+        // offsets from one base), row values and the uniform c hoisted
+        PointOps<R> v;
+        v.pb0 = __ldg(a.op.pb[0].p + y);
+        v.pb1 = __ldg(a.op.pb[1].p + y);
+        v.cc = a.coupling ? __ldg(a.op.cc.p) : C{};
+        const C* pa0 = a.op.pa[0].p + jj;
+        const C* pa1 = a.op.pa[1].p + jj;
+        const C* s01 = a.op.s01.p + jj;
+        const C* s10 = a.op.s10.p + jj;
 #pragma unroll kOpsUnroll
-      for (int m = 0; m < E / 2; ++m) {
-        const int x = jj + m * 2 * T;
-        C p0 = cscale(r0.ld(0, x), lam), p1 = cscale(r1.ld(0, x), lam);
-        real_space_ops<R>(p0, p1, x, rf, a);
-        r0.st(0, x, p0);
-        r1.st(0, x, p1);
+        for (int m = 0; m < E / 2; ++m) {
+          const int x = jj + m * 2 * T;
+          C p0 = cscale(r0.ld(0, x), lam), p1 = cscale(r1.ld(0, x), lam);
+          v.pa0 = __ldg(pa0 + m * 2 * T);
+          v.pa1 = __ldg(pa1 + m * 2 * T);
+          if (a.coupling) {
+            v.s01 = __ldg(s01 + m * 2 * T);
+            v.s10 = __ldg(s10 + m * 2 * T);
+          }
+          apply_real_ops<R>(p0, p1, v, a);
+          r0.st(0, x, p0);
+          r1.st(0, x, p1);
+        }
+      } else {
+        RowFields<R> rf;
+        rf.init(a.op, y);
+#pragma unroll kOpsUnroll
+        for (int m = 0; m < E / 2; ++m) {
+          const int x = jj + m * 2 * T;
+          C p0 = cscale(r0.ld(0, x), lam), p1 = cscale(r1.ld(0, x), lam);
+          real_space_ops<R>(p0, p1, x, rf, a);
+          r0.st(0, x, p0);
+          r1.st(0, x, p1);
+        }
       }
     }
     __syncthreads();
@@ -484,7 +568,7 @@ row_kernel(const RowArgs<R> a) {
   }
   C* out = a.out[comp];
 #pragma unroll
-  for (int m = 0; m < E; ++m) out[row_off + j + m * T] = v[0][m];
+  for (int m = 0; m < E; ++m) st_state(out + row_off + j + m * T, v[0][m]);
   (void)NT;
 }
 
@@ -518,7 +602,7 @@ col_kernel(const ColArgs<R> a) {
 #pragma unroll
   for (int m = 0; m < E; ++m) {
     const int row = j + (a.in_shift ? (m + E / 2) % E : m) * T;
-    v[0][m] = in[(long long)row * nx + xin];
+    v[0][m] = ld_state(in + (long long)row * nx + xin);
   }
   allow_next_grid();
   const LineSmem<C, E> smv{sm + c * LS, 0};
@@ -540,7 +624,7 @@ col_kernel(const ColArgs<R> a) {
 #pragma unroll
   for (int m = 0; m < E; ++m) {
     const int row = j + (a.out_shift ? (m + E / 2) % E : m) * T;
-    out[(long long)row * nx + xout] = v[0][m];
+    st_state(out + (long long)row * nx + xout, v[0][m]);
   }
   if (a.part != nullptr) {
     su = warp_sum(su);

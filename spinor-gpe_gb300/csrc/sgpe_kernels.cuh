@@ -467,7 +467,10 @@ __device__ __forceinline__ void apply_kinetic(Cx<R> (&v)[E], const KinOp<R>& k, 
 // line, so 2*T*ROWS threads.  Thread (rho, comp, j) transforms one line; the
 // point-wise operators, which couple the components, run between the
 // transforms on the natural-order rows left in shared memory.
-template <typename R, int N, int E, int ROWS, int MINB>
+// SEP selects the point-wise code at compile time (separable operator
+// tables, RealOp::sep, or the generic broadcast fields), so each kernel
+// carries one of the two loops and stays small in the instruction cache.
+template <typename R, int N, int E, int ROWS, int MINB, bool SEP>
 __global__ void __launch_bounds__(2 * (N / E) * ROWS, MINB)
 row_kernel(const RowArgs<R> a) {
   using C = Cx<R>;
@@ -519,7 +522,7 @@ row_kernel(const RowArgs<R> a) {
       const LineSmem<C, E> r0{sm + rho * LS, 0};
       const LineSmem<C, E> r1{sm + (ROWS + rho) * LS, 0};
       const int jj = tid % (2 * T);
-      if (a.op.sep) {
+      if constexpr (SEP) {
         // separable operators: x-tables read at jj + m*2T (compile-time
         // offsets from one base), row values and the uniform c hoisted
         PointOps<R> v;

@@ -144,14 +144,14 @@ inline cudaError_t launch_pdl(K kernel, dim3 grid, dim3 block, size_t smem, cuda
 #endif
 }
 
-template <typename R> struct RowLauncher {
+template <typename R, bool SEP> struct RowLauncher {
   const RowArgs<R>* a;
   int ny;
   cudaStream_t s;
   template <int N> cudaError_t run() const {
     using Cfg = RowCfg<R, N>;
     if (ny % Cfg::ROWS != 0) return cudaErrorInvalidValue;
-    auto k = row_kernel<R, N, Cfg::E, Cfg::ROWS, Cfg::MINB>;
+    auto k = row_kernel<R, N, Cfg::E, Cfg::ROWS, Cfg::MINB, SEP>;
     static unsigned long long done = 0;
     cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
     if (e != cudaSuccess) return e;
@@ -183,8 +183,9 @@ template <typename R> struct ColsQuery {
   }
 };
 
-template <typename R> cudaError_t launch_row(const RowArgs<R>& a, int nx, int ny, cudaStream_t s) {
-  return dispatch_n(nx, RowLauncher<R>{&a, ny, s});
+// Row kernels with the separable (SEP) or the generic point-wise code.
+template <typename R, bool SEP> cudaError_t launch_row_ops(const RowArgs<R>& a, int nx, int ny, cudaStream_t s) {
+  return dispatch_n(nx, RowLauncher<R, SEP>{&a, ny, s});
 }
 
 template <typename R> cudaError_t launch_col(const ColArgs<R>& a, int ny, cudaStream_t s) {
@@ -244,10 +245,20 @@ template <typename R> cudaError_t launch_copy(const CopyArgs<R>& a, cudaStream_t
 // The kernels are instantiated in separate translation units (one per
 // precision and pass) so the build compiles them in parallel.
 #ifndef SGPE_INSTANTIATE
-extern template cudaError_t launch_row<float>(const RowArgs<float>&, int, int, cudaStream_t);
-extern template cudaError_t launch_row<double>(const RowArgs<double>&, int, int, cudaStream_t);
+extern template cudaError_t launch_row_ops<float, true>(const RowArgs<float>&, int, int, cudaStream_t);
+extern template cudaError_t launch_row_ops<float, false>(const RowArgs<float>&, int, int, cudaStream_t);
+extern template cudaError_t launch_row_ops<double, true>(const RowArgs<double>&, int, int, cudaStream_t);
+extern template cudaError_t launch_row_ops<double, false>(const RowArgs<double>&, int, int, cudaStream_t);
 extern template cudaError_t launch_col<float>(const ColArgs<float>&, int, cudaStream_t);
 extern template cudaError_t launch_col<double>(const ColArgs<double>&, int, cudaStream_t);
 #endif
+
+// Row pass: the separable kernels unless the step uses generic operator
+// fields (the transform-only modes take the separable kernels, which do
+// not read the operators).
+template <typename R> cudaError_t launch_row(const RowArgs<R>& a, int nx, int ny, cudaStream_t s) {
+  if (a.mode == kRowStep && !a.op.sep) return launch_row_ops<R, false>(a, nx, ny, s);
+  return launch_row_ops<R, true>(a, nx, ny, s);
+}
 
 }  // namespace sgpe

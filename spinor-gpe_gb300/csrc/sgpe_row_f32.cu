@@ -1,7 +1,7 @@
-// Row-pass kernels, complex64: explicit instantiation.
+// Row-pass kernels, complex64, separable operators: explicit instantiation.
 #define SGPE_INSTANTIATE
 #include "sgpe_launch.cuh"
 
 namespace sgpe {
-template cudaError_t launch_row<float>(const RowArgs<float>&, int, int, cudaStream_t);
+template cudaError_t launch_row_ops<float, true>(const RowArgs<float>&, int, int, cudaStream_t);
 }  // namespace sgpe

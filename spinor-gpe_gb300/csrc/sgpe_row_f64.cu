@@ -1,7 +1,7 @@
-// Row-pass kernels, complex128: explicit instantiation.
+// Row-pass kernels, complex128, separable operators: explicit instantiation.
 #define SGPE_INSTANTIATE
 #include "sgpe_launch.cuh"
 
 namespace sgpe {
-template cudaError_t launch_row<double>(const RowArgs<double>&, int, int, cudaStream_t);
+template cudaError_t launch_row_ops<double, true>(const RowArgs<double>&, int, int, cudaStream_t);
 }  // namespace sgpe

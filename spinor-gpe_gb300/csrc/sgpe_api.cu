@@ -157,6 +157,17 @@ constexpr int kGraphSteps = 8;
 // A set of plans stepped together: their steady-state steps are captured as
 // independent branches of one CUDA graph, so the solves' kernels run
 // concurrently (sgpe_batch_steps).
+// Plans of one grid size and precision whose steady-state passes run as
+// grouped launches (one kernel for the same pass of every member).
+struct BatchGroup {
+  std::vector<int> members;  // indices into sgpe_batch::plans
+  int nx = 0, ny = 0, bits = 0;
+  void* col_args = nullptr;  // device ColArgs[3][G]: (0 -> 0), (0 -> 1), (1 -> 0)
+  void* row_args = nullptr;  // device RowArgs[2][G]: sub-steps 0, 1
+  cudaStream_t stream = nullptr;
+  cudaEvent_t join = nullptr;
+};
+
 struct sgpe_batch {
   std::vector<sgpe_plan*> plans;
   int device = 0;
@@ -165,6 +176,10 @@ struct sgpe_batch {
   std::vector<cudaEvent_t> joins;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // 1 step, kGraphSteps steps
   std::vector<unsigned long long> epoch[2];        // plans' epochs at capture
+  std::vector<BatchGroup> groups;                  // shared by both graphs
+  std::vector<unsigned long long> groups_epoch;    // plans' epochs when built
+  bool groups_built = false;
+  bool grouping = true;                            // SGPE_BATCH_GROUPING=0 disables
 };
 
 namespace {
@@ -434,9 +449,12 @@ template <typename R> const sgpe::Cx<R>* cst(const void* p) { return static_cast
 // Column pass over the state (in place) ending a sub-step and starting `sub`.
 // want_u: the populations of the state entering the pass are needed, so the
 // two kinetic half steps are applied separately (sum after the first).
-template <typename R> cudaError_t col_pass_step(sgpe_plan* p, int sub, double* pops, cudaStream_t s) {
-  const bool want_u = pops != nullptr;
-  sgpe::ColArgs<R> a{};
+// Arguments of the column pass that starts sub-step `sub` (from the plan's
+// current form and previous sub-step); false if a merged table could not be
+// allocated.
+template <typename R> bool col_step_args(sgpe_plan* p, int sub, bool want_u, sgpe::ColArgs<R>* out) {
+  sgpe::ColArgs<R>& a = *out;
+  a = sgpe::ColArgs<R>{};
   a.in[0] = cst<R>(p->s[0]);
   a.in[1] = cst<R>(p->s[1]);
   a.out[0] = st<R>(p->s[0]);
@@ -453,16 +471,23 @@ template <typename R> cudaError_t col_pass_step(sgpe_plan* p, int sub, double* p
     a.k1 = kin_op<R>(p->sub[p->prev_sub]);
     a.k2 = kin_op<R>(p->sub[sub]);
   } else {
-    if (ensure_pair(p, p->prev_sub, sub) != SGPE_OK) return cudaErrorMemoryAllocation;
+    if (ensure_pair(p, p->prev_sub, sub) != SGPE_OK) return false;
     a.nk = 1;
     a.k1 = kin_pair<R>(p->pair[p->prev_sub][sub]);
   }
   a.scale = R(1);
   a.part = reinterpret_cast<R*>(p->part);
+  return true;
+}
+
+template <typename R> cudaError_t col_pass_step(sgpe_plan* p, int sub, double* pops, cudaStream_t s) {
+  sgpe::ColArgs<R> a;
+  if (!col_step_args<R>(p, sub, pops != nullptr, &a)) return cudaErrorMemoryAllocation;
   return sgpe::launch_col<R>(a, p->ny, s);
 }
 
-template <typename R> cudaError_t row_pass_step(sgpe_plan* p, int sub, double* pops, cudaStream_t s) {
+// Arguments of the row pass of sub-step `sub`.
+template <typename R> sgpe::RowArgs<R> row_step_args(sgpe_plan* p, int sub, double* pops) {
   sgpe::RowArgs<R> a{};
   a.in[0] = cst<R>(p->s[0]);
   a.in[1] = cst<R>(p->s[1]);
@@ -481,6 +506,11 @@ template <typename R> cudaError_t row_pass_step(sgpe_plan* p, int sub, double* p
   a.op = real_op<R>(p->sub[sub], p->coupling);
   a.pops = pops;
   a.atom_num = p->atom_num;
+  return a;
+}
+
+template <typename R> cudaError_t row_pass_step(sgpe_plan* p, int sub, double* pops, cudaStream_t s) {
+  const sgpe::RowArgs<R> a = row_step_args<R>(p, sub, pops);
   return sgpe::launch_row<R>(a, p->nx, p->ny, s);
 }
 
@@ -1080,6 +1110,8 @@ int sgpe_batch_create(sgpe_batch** out, sgpe_plan* const* plans, int n_plans) {
   sgpe_batch* b = new sgpe_batch();
   b->plans.assign(plans, plans + n_plans);
   b->device = plans[0]->device;
+  const char* env = std::getenv("SGPE_BATCH_GROUPING");
+  b->grouping = !(env != nullptr && env[0] == '0');
   cudaError_t e = cudaStreamCreateWithFlags(&b->root, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
   b->joins.assign(n_plans, nullptr);
@@ -1094,11 +1126,25 @@ int sgpe_batch_create(sgpe_batch** out, sgpe_plan* const* plans, int n_plans) {
   return SGPE_OK;
 }
 
+namespace {
+void free_groups(sgpe_batch* b) {
+  for (BatchGroup& g : b->groups) {
+    if (g.col_args) cudaFree(g.col_args);
+    if (g.row_args) cudaFree(g.row_args);
+    if (g.join) cudaEventDestroy(g.join);
+    if (g.stream) cudaStreamDestroy(g.stream);
+  }
+  b->groups.clear();
+  b->groups_built = false;
+}
+}  // namespace
+
 int sgpe_batch_destroy(sgpe_batch* b) {
   if (b == nullptr) return SGPE_OK;
   DeviceGuard g(b->device);
   for (auto& x : b->graph)
     if (x) cudaGraphExecDestroy(x);
+  free_groups(b);
   for (auto& ev : b->joins)
     if (ev) cudaEventDestroy(ev);
   if (b->fork) cudaEventDestroy(b->fork);
@@ -1107,18 +1153,129 @@ int sgpe_batch_destroy(sgpe_batch* b) {
   return SGPE_OK;
 }
 
+extern "C++" {
 namespace {
-// Capture `steps` steady-state steps of every plan as parallel branches.
+// Device argument arrays of a group's steady-state passes (the same
+// arguments the plans' own steps use, so results are identical).
+template <typename R> int upload_group_args(sgpe_batch* b, BatchGroup& g) {
+  const size_t G = g.members.size();
+  std::vector<sgpe::ColArgs<R>> col(3 * G);
+  std::vector<sgpe::RowArgs<R>> row(2 * G);
+  const int prevs[3] = {0, 0, 1}, subs[3] = {0, 1, 0};
+  for (size_t i = 0; i < G; ++i) {
+    sgpe_plan* p = b->plans[g.members[i]];
+    const int saved = p->prev_sub;
+    bool ok = true;
+    for (int v = 0; v < 3 && ok; ++v) {
+      p->prev_sub = prevs[v];
+      ok = col_step_args<R>(p, subs[v], false, &col[v * G + i]);
+    }
+    p->prev_sub = saved;
+    if (!ok) return fail(SGPE_ERR_OOM, "batch: merged kinetic tables");
+    for (int sub = 0; sub < 2; ++sub) row[sub * G + i] = row_step_args<R>(p, sub, nullptr);
+  }
+  cudaError_t e = cudaMalloc(&g.col_args, sizeof(sgpe::ColArgs<R>) * col.size());
+  if (e == cudaSuccess) e = cudaMalloc(&g.row_args, sizeof(sgpe::RowArgs<R>) * row.size());
+  if (e == cudaSuccess)
+    e = cudaMemcpy(g.col_args, col.data(), sizeof(sgpe::ColArgs<R>) * col.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(g.row_args, row.data(), sizeof(sgpe::RowArgs<R>) * row.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && g.stream == nullptr) e = cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess && g.join == nullptr) e = cudaEventCreateWithFlags(&g.join, cudaEventDisableTiming);
+  return e == cudaSuccess ? SGPE_OK : cuda_fail(e, "batch group arguments");
+}
+
+// `steps` steady-state full steps of a group as grouped launches on its
+// stream: per sub-step one column-pass and one row-pass launch for all
+// members.
+template <typename R> int launch_group_steps(const BatchGroup& g, int steps) {
+  const int G = int(g.members.size());
+  const auto* col = static_cast<const sgpe::ColArgs<R>*>(g.col_args);
+  const auto* row = static_cast<const sgpe::RowArgs<R>*>(g.row_args);
+  const int cv[3] = {0, 1, 2}, rs[3] = {0, 1, 0};
+  for (int k = 0; k < steps; ++k)
+    for (int t = 0; t < 3; ++t) {
+      cudaError_t e = sgpe::launch_col_grouped<R>(col + cv[t] * G, G, g.nx, g.ny, g.stream);
+      if (e == cudaSuccess) e = sgpe::launch_row_grouped<R>(row + rs[t] * G, G, g.nx, g.ny, g.stream);
+      if (e != cudaSuccess) return cuda_fail(e, "batch grouped pass");
+    }
+  return SGPE_OK;
+}
+
+// Plans that can share grouped launches: equal size and precision, and
+// separable real-space operators in both sub-steps (the grouped row kernels
+// carry the separable point-wise code).
+void build_groups(sgpe_batch* b) {
+  std::vector<bool> taken(b->plans.size(), false);
+  for (size_t i = 0; i < b->plans.size(); ++i) {
+    if (taken[i]) continue;
+    sgpe_plan* p = b->plans[i];
+    auto sep = [](const sgpe_plan* q) {
+      for (int sub = 0; sub < 2; ++sub)
+        if (!(q->sub[sub].sep.pot && (!q->coupling || q->sub[sub].sep.cpl))) return false;
+      return true;
+    };
+    if (!b->grouping || !sep(p)) continue;
+    BatchGroup g;
+    g.nx = p->nx;
+    g.ny = p->ny;
+    g.bits = p->bits;
+    for (size_t k = i; k < b->plans.size(); ++k) {
+      const sgpe_plan* q = b->plans[k];
+      if (!taken[k] && q->nx == p->nx && q->ny == p->ny && q->bits == p->bits && sep(q)) g.members.push_back(int(k));
+    }
+    if (g.members.size() < 2) continue;
+    for (int k : g.members) taken[k] = true;
+    b->groups.push_back(g);
+  }
+}
+
+// Capture `steps` steady-state steps of every plan as parallel branches:
+// one branch per group of grouped launches, one per remaining plan.
 int capture_batch(sgpe_batch* b, int steps, cudaGraphExec_t* out) {
   for (sgpe_plan* p : b->plans)
     for (int x = 0; x < 2; ++x)
       for (int y = 0; y < 2; ++y)
         if (ensure_pair(p, x, y) != SGPE_OK) return SGPE_ERR_OOM;
+  // The groups' argument arrays are shared by the 1-step and the 8-step
+  // graph.  They are rebuilt only when some plan's operators changed; the
+  // other graph, which points at the old arrays, is dropped first.
+  std::vector<unsigned long long> now;
+  for (const sgpe_plan* p : b->plans) now.push_back(p->epoch);
+  if (!b->groups_built || b->groups_epoch != now) {
+    for (auto& x : b->graph)
+      if (x != nullptr && &x != out) {
+        cudaGraphExecDestroy(x);
+        x = nullptr;
+      }
+    free_groups(b);  // cudaFree waits for launches still reading them
+    build_groups(b);
+    for (BatchGroup& g : b->groups) {
+      const int rc = g.bits == 64 ? upload_group_args<float>(b, g) : upload_group_args<double>(b, g);
+      if (rc != SGPE_OK) {
+        free_groups(b);
+        return rc;
+      }
+    }
+    b->groups_epoch = now;
+    b->groups_built = true;
+  }
+  std::vector<bool> grouped(b->plans.size(), false);
+  for (const BatchGroup& g : b->groups)
+    for (int k : g.members) grouped[k] = true;
   cudaError_t e = cudaStreamBeginCapture(b->root, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return cuda_fail(e, "batch begin capture");
   if (e == cudaSuccess) e = cudaEventRecord(b->fork, b->root);
   int rc = SGPE_OK;
+  for (size_t i = 0; i < b->groups.size() && e == cudaSuccess && rc == SGPE_OK; ++i) {
+    BatchGroup& g = b->groups[i];
+    e = cudaStreamWaitEvent(g.stream, b->fork, 0);
+    if (e == cudaSuccess) rc = g.bits == 64 ? launch_group_steps<float>(g, steps) : launch_group_steps<double>(g, steps);
+    if (e == cudaSuccess && rc == SGPE_OK) e = cudaEventRecord(g.join, g.stream);
+    if (e == cudaSuccess && rc == SGPE_OK) e = cudaStreamWaitEvent(b->root, g.join, 0);
+  }
   for (size_t i = 0; i < b->plans.size() && e == cudaSuccess && rc == SGPE_OK; ++i) {
+    if (grouped[i]) continue;
     sgpe_plan* p = b->plans[i];
     e = cudaStreamWaitEvent(p->cap_stream, b->fork, 0);
     for (int k = 0; k < steps && e == cudaSuccess && rc == SGPE_OK; ++k)
@@ -1151,6 +1308,7 @@ bool batch_stale(const sgpe_batch* b, int k) {
   return false;
 }
 }  // namespace
+}  // extern "C++"
 
 int sgpe_batch_steps(sgpe_batch* b, int n_steps, void* stream) {
   if (b == nullptr) return fail(SGPE_ERR_ARG, "null batch");

@@ -71,9 +71,32 @@ template <int DIR, int M, class C> __device__ __forceinline__ C tw16(C a) {
   else if constexpr (m == 1) return cmul(a, cmake<C>(c1, d * s1));
   else if constexpr (m == 3) return cmul(a, cmake<C>(s1, d * c1));
   else if constexpr (m == 9) return cmul(a, cmake<C>(-c1, -d * s1));
+  else if constexpr (m == 5) return crot<DIR>(cmul(a, cmake<C>(c1, d * s1)));  // W^4 W^1
+  else if constexpr (m == 7) return crot<DIR>(cmul(a, cmake<C>(s1, d * c1)));  // W^4 W^3
   else {
     static_assert(m == 1 || m == 2 || m == 3 || m == 6 || m == 9, "unused twiddle");
     return a;
+  }
+}
+
+// multiply by exp(DIR * 2 pi i m / 32), m a compile-time constant
+template <int DIR, int M, class C> __device__ __forceinline__ C tw32(C a) {
+  using R = decltype(C::x);
+  constexpr int m = M & 31;
+  if constexpr (m % 2 == 0) {
+    return tw16<DIR, m / 2>(a);
+  } else if constexpr (m > 8) {
+    return crot<DIR>(tw32<DIR, m - 8>(a));  // exp(DIR i pi/2) = DIR * i
+  } else {
+    const R c1 = R(0.98078528040323044913);  // cos(pi/16)
+    const R s1 = R(0.19509032201612826785);  // sin(pi/16)
+    const R c3 = R(0.83146961230254523708);  // cos(3 pi/16)
+    const R s3 = R(0.55557023301960222474);  // sin(3 pi/16)
+    const R d = R(DIR);
+    if constexpr (m == 1) return cmul(a, cmake<C>(c1, d * s1));
+    else if constexpr (m == 3) return cmul(a, cmake<C>(c3, d * s3));
+    else if constexpr (m == 5) return cmul(a, cmake<C>(s3, d * c3));  // cos(5pi/16) = sin(3pi/16)
+    else return cmul(a, cmake<C>(s1, d * c1));                        // m == 7
   }
 }
 
@@ -162,6 +185,41 @@ template <int DIR> struct Dft<16, DIR> {
   }
 };
 
+template <int DIR> struct Dft<32, DIR> {
+  template <class C> __device__ __forceinline__ static void run(C* a) {
+    // decimation in time: DFT16 of the even and of the odd points, then
+    // a[k] = e[k] + W32^k o[k], a[k + 16] = e[k] - W32^k o[k]
+    C e[16], o[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      e[k] = a[2 * k];
+      o[k] = a[2 * k + 1];
+    }
+    Dft<16, DIR>::run(e);
+    Dft<16, DIR>::run(o);
+    o[1] = tw32<DIR, 1>(o[1]);
+    o[2] = tw32<DIR, 2>(o[2]);
+    o[3] = tw32<DIR, 3>(o[3]);
+    o[4] = tw32<DIR, 4>(o[4]);
+    o[5] = tw32<DIR, 5>(o[5]);
+    o[6] = tw32<DIR, 6>(o[6]);
+    o[7] = tw32<DIR, 7>(o[7]);
+    o[8] = tw32<DIR, 8>(o[8]);
+    o[9] = tw32<DIR, 9>(o[9]);
+    o[10] = tw32<DIR, 10>(o[10]);
+    o[11] = tw32<DIR, 11>(o[11]);
+    o[12] = tw32<DIR, 12>(o[12]);
+    o[13] = tw32<DIR, 13>(o[13]);
+    o[14] = tw32<DIR, 14>(o[14]);
+    o[15] = tw32<DIR, 15>(o[15]);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      a[k] = cadd(e[k], o[k]);
+      a[k + 16] = csub(e[k], o[k]);
+    }
+  }
+};
+
 // Radix of the stage with sub-length NS of an (N, E) transform.  Powers of
 // two: E per stage, the remainder last.  N = 3 * 2^k: power-of-two stages of
 // at most P (the largest power of two dividing E), then one radix-3 stage.
@@ -192,12 +250,17 @@ __host__ __device__ constexpr int tw_offset(int N, int E, int NS) {
 // Shared-memory view used by the exchange stages: element i of line l of the
 // calling thread's group lives at base[l * line_stride + i + i / E] (one pad
 // element per E elements keeps the radix-E scatter free of bank conflicts).
-template <class C, int E> struct LineSmem {
+// WARP: every line is held by threads of one warp (T divides 32), so the
+// exchange between stages needs only a warp barrier.
+template <class C, int E, bool WARP = false> struct LineSmem {
   C* base;
   int line_stride;
   __device__ __forceinline__ C ld(int l, int i) const { return base[l * line_stride + i + i / E]; }
   __device__ __forceinline__ void st(int l, int i, C v) const { base[l * line_stride + i + i / E] = v; }
-  __device__ __forceinline__ void sync() const { __syncthreads(); }
+  __device__ __forceinline__ void sync() const {
+    if constexpr (WARP) __syncwarp();
+    else __syncthreads();
+  }
 };
 
 // One Stockham stage (and, recursively, the stages after it) on L lines.

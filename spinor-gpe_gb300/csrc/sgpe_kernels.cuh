@@ -470,9 +470,8 @@ __device__ __forceinline__ void apply_kinetic(Cx<R> (&v)[E], const KinOp<R>& k, 
 // SEP selects the point-wise code at compile time (separable operator
 // tables, RealOp::sep, or the generic broadcast fields), so each kernel
 // carries one of the two loops and stays small in the instruction cache.
-template <typename R, int N, int E, int ROWS, int MINB, bool SEP>
-__global__ void __launch_bounds__(2 * (N / E) * ROWS, MINB)
-row_kernel(const RowArgs<R> a) {
+template <typename R, int N, int E, int ROWS, bool SEP>
+__device__ __forceinline__ void row_body(const RowArgs<R>& a) {
   using C = Cx<R>;
   constexpr int T = N / E;
   constexpr int LS = N + N / E;
@@ -494,8 +493,9 @@ row_kernel(const RowArgs<R> a) {
 #pragma unroll
   for (int m = 0; m < E; ++m) v[0][m] = ld_state(in + row_off + j + m * T);
   allow_next_grid();
-  // line (comp, rho) at sm + (comp*ROWS + rho)*LS
-  const LineSmem<C, E> smv{sm + (comp * ROWS + rho) * LS, 0};
+  // line (comp, rho) at sm + (comp*ROWS + rho)*LS; a line's T threads lie in
+  // one warp when T divides 32 (the transforms then synchronise per warp)
+  const LineSmem<C, E, (32 % T == 0)> smv{sm + (comp * ROWS + rho) * LS, 0};
 
   if (a.mode == kRowStep) {
     // inverse x transform, result left in shared memory (natural order)
@@ -575,10 +575,23 @@ row_kernel(const RowArgs<R> a) {
   (void)NT;
 }
 
+template <typename R, int N, int E, int ROWS, int MINB, bool SEP>
+__global__ void __launch_bounds__(2 * (N / E) * ROWS, MINB)
+row_kernel(const RowArgs<R> a) {
+  row_body<R, N, E, ROWS, SEP>(a);
+}
+
+// Several solves of one size in one launch (a batch): blockIdx.y selects the
+// solve's arguments.
+template <typename R, int N, int E, int ROWS, int MINB, bool SEP>
+__global__ void __launch_bounds__(2 * (N / E) * ROWS, MINB)
+row_kernel_grouped(const RowArgs<R>* __restrict__ args) {
+  row_body<R, N, E, ROWS, SEP>(args[blockIdx.y]);
+}
+
 // -------------------------------------------------------------- column pass
-template <typename R, int N, int E, int COLS, int MINB>
-__global__ void __launch_bounds__((N / E) * COLS, MINB)
-col_kernel(const ColArgs<R> a) {
+template <typename R, int N, int E, int COLS>
+__device__ __forceinline__ void col_body(const ColArgs<R>& a) {
   using C = Cx<R>;
   constexpr int T = N / E;
   constexpr int LS = N + N / E + 2;
@@ -650,6 +663,19 @@ col_kernel(const ColArgs<R> a) {
       }
     }
   }
+}
+
+template <typename R, int N, int E, int COLS, int MINB>
+__global__ void __launch_bounds__((N / E) * COLS, MINB)
+col_kernel(const ColArgs<R> a) {
+  col_body<R, N, E, COLS>(a);
+}
+
+// Several solves of one size in one launch: blockIdx.z selects the solve.
+template <typename R, int N, int E, int COLS, int MINB>
+__global__ void __launch_bounds__((N / E) * COLS, MINB)
+col_kernel_grouped(const ColArgs<R>* __restrict__ args) {
+  col_body<R, N, E, COLS>(args[blockIdx.z]);
 }
 
 // Final k-space renormalisation of a materialised psik

@@ -18,6 +18,14 @@ template <typename R> struct Tune;
 #ifndef SGPE_F32_ROW_E
 #define SGPE_F32_ROW_E 16
 #endif
+// Points per thread of the row transforms for sides >= 2048 (longer lines
+// spill with larger E).
+#ifndef SGPE_F32_ROW_E_LARGE
+#define SGPE_F32_ROW_E_LARGE 16
+#endif
+#ifndef SGPE_F32_ROW_MINB_LARGE
+#define SGPE_F32_ROW_MINB_LARGE 8
+#endif
 #ifndef SGPE_F32_ROW_THREADS
 #define SGPE_F32_ROW_THREADS 128
 #endif
@@ -46,11 +54,13 @@ template <typename R> struct Tune;
 #endif
 template <> struct Tune<float> {
   static constexpr int ROW_E = SGPE_F32_ROW_E, ROW_THREADS = SGPE_F32_ROW_THREADS, ROW_MINB = SGPE_F32_ROW_MINB;
+  static constexpr int ROW_E_LARGE = SGPE_F32_ROW_E_LARGE, ROW_MINB_LARGE = SGPE_F32_ROW_MINB_LARGE;
   static constexpr int COL_E = SGPE_F32_COL_E, COLS = SGPE_F32_COLS, COL_MINB = SGPE_F32_COL_MINB;
   static constexpr int R3_E = SGPE_F32_R3_E, R3_ROW_MINB = SGPE_F32_R3_ROW_MINB, R3_COL_MINB = SGPE_F32_R3_COL_MINB;
 };
 template <> struct Tune<double> {
   static constexpr int ROW_E = 8, ROW_THREADS = 256, ROW_MINB = 2;
+  static constexpr int ROW_E_LARGE = 8, ROW_MINB_LARGE = 2;
   static constexpr int COL_E = 8, COLS = 4, COL_MINB = 1;
   static constexpr int R3_E = 12, R3_ROW_MINB = 2, R3_COL_MINB = 1;
 };
@@ -65,14 +75,15 @@ template <typename R> constexpr int pick_e(int n, int e_pow2) {
 }
 
 template <typename R, int N> struct RowCfg {
-  static constexpr int E = pick_e<R>(N, Tune<R>::ROW_E);
+  static constexpr int E = pick_e<R>(N, N >= 2048 ? Tune<R>::ROW_E_LARGE : Tune<R>::ROW_E);
   static constexpr int T = N / E;
   // threads: 2 components x T per row; at least one warp, at most 16 rows
   static constexpr int ROWS = cmax(cmax(cmin(Tune<R>::ROW_THREADS / (2 * T), 16), 1), 32 / (2 * T));
   static constexpr int THREADS = 2 * T * ROWS;
   static constexpr size_t SMEM = 2ull * ROWS * (N + N / E) * sizeof(Cx<R>);
   static constexpr int MINB =
-      cmax(1, cmin(N % 3 == 0 ? Tune<R>::R3_ROW_MINB : Tune<R>::ROW_MINB, 1024 / THREADS));
+      cmax(1, cmin(N % 3 == 0 ? Tune<R>::R3_ROW_MINB : N >= 2048 ? Tune<R>::ROW_MINB_LARGE : Tune<R>::ROW_MINB,
+                   1024 / THREADS));
 };
 
 template <typename R, int N> struct ColCfg {
@@ -175,6 +186,38 @@ template <typename R> struct ColLauncher {
   }
 };
 
+// Grouped launches: G solves of the same size in one launch, per-solve
+// arguments in device memory (blockIdx.y / blockIdx.z selects the solve).
+template <typename R, bool SEP> struct RowGroupedLauncher {
+  const RowArgs<R>* args;
+  int groups, ny;
+  cudaStream_t s;
+  template <int N> cudaError_t run() const {
+    using Cfg = RowCfg<R, N>;
+    if (ny % Cfg::ROWS != 0) return cudaErrorInvalidValue;
+    auto k = row_kernel_grouped<R, N, Cfg::E, Cfg::ROWS, Cfg::MINB, SEP>;
+    static unsigned long long done = 0;
+    cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
+    if (e != cudaSuccess) return e;
+    return launch_pdl(k, dim3(ny / Cfg::ROWS, groups), dim3(Cfg::THREADS), Cfg::SMEM, s, args);
+  }
+};
+
+template <typename R> struct ColGroupedLauncher {
+  const ColArgs<R>* args;
+  int groups, nx;
+  cudaStream_t s;
+  template <int N> cudaError_t run() const {
+    using Cfg = ColCfg<R, N>;
+    if (nx % Cfg::COLS != 0 || (nx / 2) % Cfg::COLS != 0) return cudaErrorInvalidValue;
+    auto k = col_kernel_grouped<R, N, Cfg::E, Cfg::COLS, Cfg::MINB>;
+    static unsigned long long done = 0;
+    cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
+    if (e != cudaSuccess) return e;
+    return launch_pdl(k, dim3(nx / Cfg::COLS, 2, groups), dim3(Cfg::THREADS), Cfg::SMEM, s, args);
+  }
+};
+
 template <typename R> struct ColsQuery {
   int* out;
   template <int N> cudaError_t run() const {
@@ -190,6 +233,16 @@ template <typename R, bool SEP> cudaError_t launch_row_ops(const RowArgs<R>& a, 
 
 template <typename R> cudaError_t launch_col(const ColArgs<R>& a, int ny, cudaStream_t s) {
   return dispatch_n(ny, ColLauncher<R>{&a, ny, s});
+}
+
+// `args` in device memory, `groups` solves of an (ny, nx) grid.
+template <typename R> cudaError_t launch_row_grouped(const RowArgs<R>* args, int groups, int nx, int ny,
+                                                     cudaStream_t s) {
+  return dispatch_n(nx, RowGroupedLauncher<R, true>{args, groups, ny, s});
+}
+template <typename R> cudaError_t launch_col_grouped(const ColArgs<R>* args, int groups, int nx, int ny,
+                                                     cudaStream_t s) {
+  return dispatch_n(ny, ColGroupedLauncher<R>{args, groups, nx, s});
 }
 
 template <typename R> struct RowEQuery {
@@ -251,6 +304,10 @@ extern template cudaError_t launch_row_ops<double, true>(const RowArgs<double>&,
 extern template cudaError_t launch_row_ops<double, false>(const RowArgs<double>&, int, int, cudaStream_t);
 extern template cudaError_t launch_col<float>(const ColArgs<float>&, int, cudaStream_t);
 extern template cudaError_t launch_col<double>(const ColArgs<double>&, int, cudaStream_t);
+extern template cudaError_t launch_row_grouped<float>(const RowArgs<float>*, int, int, int, cudaStream_t);
+extern template cudaError_t launch_row_grouped<double>(const RowArgs<double>*, int, int, int, cudaStream_t);
+extern template cudaError_t launch_col_grouped<float>(const ColArgs<float>*, int, int, int, cudaStream_t);
+extern template cudaError_t launch_col_grouped<double>(const ColArgs<double>*, int, int, int, cudaStream_t);
 #endif
 
 // Row pass: the separable kernels unless the step uses generic operator

@@ -1,0 +1,7 @@
+// Grouped (batched) row-pass kernels, complex128: explicit instantiation.
+#define SGPE_INSTANTIATE
+#include "sgpe_launch.cuh"
+
+namespace sgpe {
+template cudaError_t launch_row_grouped<double>(const RowArgs<double>*, int, int, int, cudaStream_t);
+}  // namespace sgpe

@@ -418,3 +418,36 @@ def test_batch_matches_solves_alone(tp, tmp_path):
     batch.full_steps(9)
     same()
     batch.close()
+
+
+@pytest.mark.parametrize('grouping', ['1', '0'])
+def test_grouped_batch_matches_solves_alone(tp, tmp_path, monkeypatch, grouping):
+    """Solves of one size and precision run as grouped launches (one kernel
+    per pass for all of them); with grouping on or off every solve equals
+    the same solve stepped alone, bit for bit."""
+    from spinor_gpe import workloads
+    from spinor_gpe.batch import PropagatorBatch
+    from spinor_gpe.pspinor import pspinor as spin
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    monkeypatch.setenv('SGPE_BATCH_GROUPING', grouping)
+    spins = workloads.batched_uneven(spin.PSpinor, ttools.fft_2d,
+                                     str(tmp_path) + '/g/', n_solves=6,
+                                     sizes=(128,), seed=11)
+    spins += workloads.batched_uneven(spin.PSpinor, ttools.fft_2d,
+                                      str(tmp_path) + '/h/', n_solves=1,
+                                      sizes=(256,), seed=12)
+    kinds = [('imag', 64)] * 4 + [('real', 64)] * 2 + [('imag', 64)]
+
+    def make():
+        return [tp.TensorPropagator(s, 0.02 if t == 'imag' else 1e-3, 20, 'cuda',
+                                    time=t, dtype=d)
+                for s, (t, d) in zip(spins, kinds)]
+    alone, together = make(), make()
+    for p in alone:
+        p.full_steps(21)
+    batch = PropagatorBatch(together)
+    batch.full_steps(21)
+    for a, b in zip(alone, together):
+        np.testing.assert_array_equal(np.array([t.cpu().numpy() for t in a.psik]),
+                                      np.array([t.cpu().numpy() for t in b.psik]))
+    batch.close()

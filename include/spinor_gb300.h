@@ -191,6 +191,16 @@ int sgpe_batch_destroy(sgpe_batch* batch);
  * stepping each plan alone with sgpe_full_steps. */
 int sgpe_batch_steps(sgpe_batch* batch, int n_steps, void* stream);
 
+/* Arithmetic of the radix-16 DFT stages of the plan's transforms:
+ * mode 0 (default) FP32 butterflies on the CUDA cores; mode 1 split-BF16
+ * products on the tensor cores (each FP32 operand split into BF16 head and
+ * tail, products hi.hi + hi.lo + lo.hi accumulated in FP32), a precision-
+ * study variant for complex64 plans with sides 64, 256, 1024 or 2048.
+ * Twiddles, point-wise operators and reductions are unchanged.  The state
+ * is kept; must not be called while populations of a step are pending.
+ * No counterpart in the original. */
+int sgpe_set_dft_mode(sgpe_plan* plan, int mode);
+
 /* Size in bytes of the device scratch array used by sgpe_fft2_static
  * (2.25 MiB, present on every GPU that loads the library). */
 #define SGPE_FFT2_STATIC_BYTES (2359296)

@@ -122,7 +122,10 @@ struct sgpe_plan {
   void* s[2] = {nullptr, nullptr};
   void* scratch[2] = {nullptr, nullptr};
   double* part = nullptr;    // column-pass partial sums [2][ntile][2]
-  int ntile = 0;
+  int ntile = 0;             // column tiles of the current kernels
+  int ntile_fp32 = 0;        // ... of the FP32 DFT kernels
+  int tc = 0;                // radix-16 stages on the tensor cores (split-BF16)
+  uint32_t* tcb = nullptr;   // their B fragments (device)
   void* tw_x = nullptr;
   void* tw_y = nullptr;
   SubOps sub[2];
@@ -460,6 +463,8 @@ template <typename R> bool col_step_args(sgpe_plan* p, int sub, bool want_u, sgp
   a.out[0] = st<R>(p->s[0]);
   a.out[1] = st<R>(p->s[1]);
   a.tw = cst<R>(p->tw_y);
+  a.tc = p->tc;
+  a.tcb = p->tcb;
   a.nx = p->nx;
   a.fwd = (p->form == kMixed);
   a.inv = 1;
@@ -494,6 +499,8 @@ template <typename R> sgpe::RowArgs<R> row_step_args(sgpe_plan* p, int sub, doub
   a.out[0] = st<R>(p->s[0]);
   a.out[1] = st<R>(p->s[1]);
   a.tw = cst<R>(p->tw_x);
+  a.tc = p->tc;
+  a.tcb = p->tcb;
   a.mode = sgpe::kRowStep;
   a.scale = R(1);
   a.part = reinterpret_cast<R*>(p->part);
@@ -547,6 +554,8 @@ template <typename R> int store(sgpe_plan* p, void* o0, void* o1, double* pops, 
   a.out[0] = st<R>(o0);
   a.out[1] = st<R>(o1);
   a.tw = cst<R>(p->tw_y);
+  a.tc = p->tc;
+  a.tcb = p->tcb;
   a.nx = p->nx;
   a.fwd = 1;
   a.inv = 0;
@@ -581,8 +590,12 @@ template <typename R> int fft2(sgpe_plan* p, const void* i0, const void* i1, voi
   }
   sgpe::RowArgs<R> r{};
   r.tw = cst<R>(p->tw_x);
+  r.tc = p->tc;
+  r.tcb = p->tcb;
   sgpe::ColArgs<R> c{};
   c.tw = cst<R>(p->tw_y);
+  c.tc = p->tc;
+  c.tcb = p->tcb;
   c.nx = p->nx;
   c.scale = R(1);
   cudaError_t e;
@@ -780,9 +793,11 @@ int sgpe_plan_create(sgpe_plan** out, int ny, int nx, int dtype_bits, int device
     return fail(SGPE_ERR_ARG, "nx incompatible with the column tile width");
   }
   p->ntile = nx / cols;
+  p->ntile_fp32 = p->ntile;
   cudaError_t e = cudaSuccess;
   for (int c = 0; c < 2 && e == cudaSuccess; ++c) e = cudaMalloc(&p->s[c], p->elem * (size_t)nx * ny);
-  const size_t red_bytes = sizeof(double) * 4 * (size_t)p->ntile;
+  // room for one tile per column: every kernel configuration fits
+  const size_t red_bytes = sizeof(double) * 4 * (size_t)nx;
   if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&p->part), red_bytes);
   if (e == cudaSuccess) e = cudaMemset(p->part, 0, red_bytes);
   if (e == cudaSuccess) {
@@ -823,7 +838,48 @@ int sgpe_plan_destroy(sgpe_plan* p) {
   for (int c = 0; c < 2; ++c)
     if (p->epsi[c]) cudaFree(p->epsi[c]);
   if (p->epart) cudaFree(p->epart);
+  if (p->tcb) cudaFree(p->tcb);
   delete p;
+  return SGPE_OK;
+}
+
+}  // extern "C"
+
+namespace {
+__global__ void __launch_bounds__(256) tc_bfrag_kernel(uint32_t* bfrag) {
+  sgpe::tc_fill_bfrag(bfrag, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+}  // namespace
+
+extern "C" {
+
+int sgpe_set_dft_mode(sgpe_plan* p, int mode) {
+  if (p == nullptr) return fail(SGPE_ERR_ARG, "null plan");
+  if (mode != 0 && mode != 1) return fail(SGPE_ERR_ARG, "dft mode must be 0 (FP32) or 1 (split-BF16 tensor cores)");
+  if (mode == 1) {
+    if (p->bits != 64) return fail(SGPE_ERR_ARG, "the tensor-core DFT16 variant is complex64 only");
+    if (!sgpe::tc_size_supported(p->nx) || !sgpe::tc_size_supported(p->ny))
+      return fail(SGPE_ERR_ARG, "the tensor-core DFT16 variant supports sides 64, 256, 1024 and 2048");
+  }
+  if (p->form == kMixed && p->pending_pops != nullptr)
+    return fail(SGPE_ERR_STATE, "populations of the last step are pending; read the state first");
+  if (mode == 1 && p->tcb == nullptr) {
+    DeviceGuard g(p->device);
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p->tcb), sizeof(uint32_t) * sgpe::kTcBfragWords);
+    if (e == cudaSuccess) {
+      tc_bfrag_kernel<<<8, 256>>>(p->tcb);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+      if (p->tcb) cudaFree(p->tcb);
+      p->tcb = nullptr;
+      return cuda_fail(e, "tensor-core DFT tables");
+    }
+  }
+  p->tc = mode;
+  p->ntile = mode ? p->nx / sgpe::tc_col_tile_width(p->ny) : p->ntile_fp32;
+  drop_graphs(p);
   return SGPE_OK;
 }
 
@@ -1211,6 +1267,7 @@ void build_groups(sgpe_batch* b) {
     if (taken[i]) continue;
     sgpe_plan* p = b->plans[i];
     auto sep = [](const sgpe_plan* q) {
+      if (q->tc) return false;  // the grouped kernels carry the FP32 DFTs
       for (int sub = 0; sub < 2; ++sub)
         if (!(q->sub[sub].sep.pot && (!q->coupling || q->sub[sub].sep.cpl))) return false;
       return true;

@@ -26,6 +26,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "sgpe_tc.cuh"
+
 namespace sgpe {
 
 template <typename R> struct CxT;
@@ -252,9 +254,13 @@ __host__ __device__ constexpr int tw_offset(int N, int E, int NS) {
 // element per E elements keeps the radix-E scatter free of bank conflicts).
 // WARP: every line is held by threads of one warp (T divides 32), so the
 // exchange between stages needs only a warp barrier.
-template <class C, int E, bool WARP = false> struct LineSmem {
+// TC: radix-16 stages take their DFT16 on the tensor cores (split-BF16,
+// sgpe_tc.cuh) with the staging area in `tc`.
+template <class C, int E, bool WARP = false, bool TC = false> struct LineSmem {
+  static constexpr bool kTc = TC;
   C* base;
   int line_stride;
+  TcScratch tc;
   __device__ __forceinline__ C ld(int l, int i) const { return base[l * line_stride + i + i / E]; }
   __device__ __forceinline__ void st(int l, int i, C v) const { base[l * line_stride + i + i / E] = v; }
   __device__ __forceinline__ void sync() const {
@@ -305,7 +311,10 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
 #pragma unroll
   for (int l = 0; l < L; ++l)
 #pragma unroll
-    for (int q = 0; q < Q; ++q) Dft<R, DIR>::run(a[l][q]);
+    for (int q = 0; q < Q; ++q) {
+      if constexpr (SM::kTc && R == 16) tc_dft16<DIR>(a[l][q], sm.tc);
+      else Dft<R, DIR>::run(a[l][q]);
+    }
   if constexpr (kLast && !TO_SMEM) {
 #pragma unroll
     for (int l = 0; l < L; ++l)

@@ -177,6 +177,8 @@ template <typename R> struct RowArgs {
   double* pops;           // non-null: block 0 writes the populations of the
                           // state the preceding column pass started from
   double atom_num;
+  int tc;                 // launch the tensor-core DFT16 kernels (host side)
+  const uint32_t* tcb;    // their B fragments (kTcBfragWords, device)
 };
 
 template <typename R> struct ColArgs {
@@ -193,6 +195,8 @@ template <typename R> struct ColArgs {
   R* part;                // non-null: per-block partial sums [comp][tile][u, w]
                           // in the working precision; the consumer of the
                           // pass sums them with (at least) FP64 accuracy
+  int tc;                 // launch the tensor-core DFT16 kernels (host side)
+  const uint32_t* tcb;    // their B fragments (kTcBfragWords, device)
 };
 
 template <typename R> struct ScaleArgs {
@@ -467,12 +471,35 @@ __device__ __forceinline__ void apply_kinetic(Cx<R> (&v)[E], const KinOp<R>& k, 
 // line, so 2*T*ROWS threads.  Thread (rho, comp, j) transforms one line; the
 // point-wise operators, which couple the components, run between the
 // transforms on the natural-order rows left in shared memory.
+// Tensor-core DFT16 staging for a block whose exchange area takes
+// `exchange_bytes`: B fragments after it (16-byte aligned), copied from the
+// plan's table `tcb`, then one tile per warp.  Every thread copies its share
+// of the fragments; the caller synchronises the block before the first
+// transform.
+template <bool TC>
+__device__ __forceinline__ TcScratch tc_setup(unsigned char* smem_raw, size_t exchange_bytes, const uint32_t* tcb,
+                                              int tid, int nthreads) {
+  TcScratch t{};
+  if constexpr (TC) {
+    const size_t off = (exchange_bytes + 15) & ~size_t(15);
+    uint32_t* bfrag = reinterpret_cast<uint32_t*>(smem_raw + off);
+    // copy of the plan's B fragments (tc_fill_bfrag, computed once)
+    for (int i = tid; i < kTcBfragWords / 4; i += nthreads)
+      reinterpret_cast<uint4*>(bfrag)[i] = __ldg(reinterpret_cast<const uint4*>(tcb) + i);
+    t.bfrag = bfrag;
+    t.tile = reinterpret_cast<float*>(smem_raw + off + sizeof(uint32_t) * kTcBfragWords) + (tid >> 5) * kTcScratchFloats;
+  }
+  return t;
+}
+
 // SEP selects the point-wise code at compile time (separable operator
 // tables, RealOp::sep, or the generic broadcast fields), so each kernel
 // carries one of the two loops and stays small in the instruction cache.
-template <typename R, int N, int E, int ROWS, bool SEP>
+// TC: radix-16 stages on the tensor cores (complex64 only).
+template <typename R, int N, int E, int ROWS, bool SEP, bool TC = false>
 __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
   using C = Cx<R>;
+  static_assert(!TC || sizeof(R) == 4, "tensor-core DFT16 is complex64 only");
   constexpr int T = N / E;
   constexpr int LS = N + N / E;
   constexpr int NT = 2 * T * ROWS;
@@ -481,6 +508,8 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
   __shared__ R s_lambda;
 
   const int tid = threadIdx.x;
+  const TcScratch tcs = tc_setup<TC>(smem_raw, sizeof(C) * 2 * ROWS * LS, a.tcb, tid, NT);
+  if constexpr (TC) __syncthreads();
   const int rho = tid / (2 * T);
   const int comp = (tid / T) & 1;
   const int j = tid % T;
@@ -495,7 +524,7 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
   allow_next_grid();
   // line (comp, rho) at sm + (comp*ROWS + rho)*LS; a line's T threads lie in
   // one warp when T divides 32 (the transforms then synchronise per warp)
-  const LineSmem<C, E, (32 % T == 0)> smv{sm + (comp * ROWS + rho) * LS, 0};
+  const LineSmem<C, E, (32 % T == 0), TC> smv{sm + (comp * ROWS + rho) * LS, 0, tcs};
 
   if (a.mode == kRowStep) {
     // inverse x transform, result left in shared memory (natural order)
@@ -575,10 +604,10 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
   (void)NT;
 }
 
-template <typename R, int N, int E, int ROWS, int MINB, bool SEP>
+template <typename R, int N, int E, int ROWS, int MINB, bool SEP, bool TC = false>
 __global__ void __launch_bounds__(2 * (N / E) * ROWS, MINB)
 row_kernel(const RowArgs<R> a) {
-  row_body<R, N, E, ROWS, SEP>(a);
+  row_body<R, N, E, ROWS, SEP, TC>(a);
 }
 
 // Several solves of one size in one launch (a batch): blockIdx.y selects the
@@ -590,9 +619,10 @@ row_kernel_grouped(const RowArgs<R>* __restrict__ args) {
 }
 
 // -------------------------------------------------------------- column pass
-template <typename R, int N, int E, int COLS>
+template <typename R, int N, int E, int COLS, bool TC = false>
 __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
   using C = Cx<R>;
+  static_assert(!TC || sizeof(R) == 4, "tensor-core DFT16 is complex64 only");
   constexpr int T = N / E;
   constexpr int LS = N + N / E + 2;
   constexpr int NT = T * COLS;
@@ -602,6 +632,8 @@ __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
   __shared__ R s_red[2][NW];
 
   const int tid = threadIdx.x;
+  const TcScratch tcs = tc_setup<TC>(smem_raw, sizeof(C) * COLS * LS, a.tcb, tid, NT);
+  if constexpr (TC) __syncthreads();
   const int c = tid % COLS;
   const int j = tid / COLS;
   const int comp = blockIdx.y;
@@ -621,7 +653,7 @@ __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
     v[0][m] = ld_state(in + (long long)row * nx + xin);
   }
   allow_next_grid();
-  const LineSmem<C, E> smv{sm + c * LS, 0};
+  const LineSmem<C, E, false, TC> smv{sm + c * LS, 0, tcs};
   if (a.fwd) fft_lines<N, E, -1, 1>(v, j, smv, a.tw);
 
   R su = R(0), sw = R(0);
@@ -665,10 +697,10 @@ __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
   }
 }
 
-template <typename R, int N, int E, int COLS, int MINB>
+template <typename R, int N, int E, int COLS, int MINB, bool TC = false>
 __global__ void __launch_bounds__((N / E) * COLS, MINB)
 col_kernel(const ColArgs<R> a) {
-  col_body<R, N, E, COLS>(a);
+  col_body<R, N, E, COLS, TC>(a);
 }
 
 // Several solves of one size in one launch: blockIdx.z selects the solve.

@@ -186,6 +186,91 @@ template <typename R> struct ColLauncher {
   }
 };
 
+// Tensor-core DFT16 variant (complex64; sides with radix-16 stages:
+// 64, 256, 1024, 2048).  Rows: the row configuration with a 128-register
+// cap; columns: 4 columns per block (at least one warp), so the staging
+// tiles of every warp fit in shared memory at 2048.
+inline bool tc_size_supported(int n) { return n == 64 || n == 256 || n == 1024 || n == 2048; }
+
+template <int N> struct RowTcCfg {
+  using B = RowCfg<float, N>;
+  static constexpr int E = B::E, ROWS = B::ROWS, THREADS = B::THREADS;
+  static constexpr int MINB = cmax(1, cmin(2, 1024 / THREADS));
+  static constexpr size_t SMEM = ((B::SMEM + 15) & ~size_t(15)) + sizeof(uint32_t) * kTcBfragWords +
+                                 size_t(THREADS / 32) * kTcScratchFloats * sizeof(float);
+};
+
+template <int N> struct ColTcCfg {
+  static constexpr int E = pick_e<float>(N, Tune<float>::COL_E);
+  static constexpr int T = N / E;
+  static constexpr int COLS = cmax(4, 32 / T);
+  static constexpr int THREADS = T * COLS;
+  static constexpr int MINB = 1;
+  static constexpr size_t XBYTES = size_t(COLS) * (N + N / E + 2) * sizeof(float2);
+  static constexpr size_t SMEM = ((XBYTES + 15) & ~size_t(15)) + sizeof(uint32_t) * kTcBfragWords +
+                                 size_t(THREADS / 32) * kTcScratchFloats * sizeof(float);
+};
+
+template <class F> inline cudaError_t dispatch_tc(int n, F&& f) {
+  switch (n) {
+    case 64: return f.template run<64>();
+    case 256: return f.template run<256>();
+    case 1024: return f.template run<1024>();
+    case 2048: return f.template run<2048>();
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+struct RowTcLauncher {
+  const RowArgs<float>* a;
+  int ny;
+  cudaStream_t s;
+  template <int N> cudaError_t run() const {
+    using Cfg = RowTcCfg<N>;
+    if (ny % Cfg::ROWS != 0) return cudaErrorInvalidValue;
+    auto k = row_kernel<float, N, Cfg::E, Cfg::ROWS, Cfg::MINB, true, true>;
+    static unsigned long long done = 0;
+    cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
+    if (e != cudaSuccess) return e;
+    return launch_pdl(k, dim3(ny / Cfg::ROWS), dim3(Cfg::THREADS), Cfg::SMEM, s, *a);
+  }
+};
+
+struct ColTcLauncher {
+  const ColArgs<float>* a;
+  int ny;
+  cudaStream_t s;
+  template <int N> cudaError_t run() const {
+    using Cfg = ColTcCfg<N>;
+    const int nx = a->nx;
+    if (nx % Cfg::COLS != 0 || (nx / 2) % Cfg::COLS != 0) return cudaErrorInvalidValue;
+    auto k = col_kernel<float, N, Cfg::E, Cfg::COLS, Cfg::MINB, true>;
+    static unsigned long long done = 0;
+    cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
+    if (e != cudaSuccess) return e;
+    return launch_pdl(k, dim3(nx / Cfg::COLS, 2), dim3(Cfg::THREADS), Cfg::SMEM, s, *a);
+  }
+};
+
+cudaError_t launch_row_tc(const RowArgs<float>& a, int nx, int ny, cudaStream_t s);  // sgpe_tc_f32.cu
+cudaError_t launch_col_tc(const ColArgs<float>& a, int ny, cudaStream_t s);
+inline cudaError_t launch_row_tc(const RowArgs<double>&, int, int, cudaStream_t) { return cudaErrorInvalidValue; }
+inline cudaError_t launch_col_tc(const ColArgs<double>&, int, cudaStream_t) { return cudaErrorInvalidValue; }
+
+struct ColTcColsQuery {
+  int* out;
+  template <int N> cudaError_t run() const {
+    *out = ColTcCfg<N>::COLS;
+    return cudaSuccess;
+  }
+};
+// Column-tile width of the tensor-core column kernels (0 if unsupported).
+inline int tc_col_tile_width(int ny) {
+  int c = 0;
+  if (dispatch_tc(ny, ColTcColsQuery{&c}) != cudaSuccess) return 0;
+  return c;
+}
+
 // Grouped launches: G solves of the same size in one launch, per-solve
 // arguments in device memory (blockIdx.y / blockIdx.z selects the solve).
 template <typename R, bool SEP> struct RowGroupedLauncher {
@@ -232,6 +317,7 @@ template <typename R, bool SEP> cudaError_t launch_row_ops(const RowArgs<R>& a, 
 }
 
 template <typename R> cudaError_t launch_col(const ColArgs<R>& a, int ny, cudaStream_t s) {
+  if (a.tc) return launch_col_tc(a, ny, s);
   return dispatch_n(ny, ColLauncher<R>{&a, ny, s});
 }
 
@@ -314,6 +400,10 @@ extern template cudaError_t launch_col_grouped<double>(const ColArgs<double>*, i
 // fields (the transform-only modes take the separable kernels, which do
 // not read the operators).
 template <typename R> cudaError_t launch_row(const RowArgs<R>& a, int nx, int ny, cudaStream_t s) {
+  if (a.tc) {
+    if (a.mode == kRowStep && !a.op.sep) return cudaErrorInvalidValue;  // not instantiated
+    return launch_row_tc(a, nx, ny, s);
+  }
   if (a.mode == kRowStep && !a.op.sep) return launch_row_ops<R, false>(a, nx, ny, s);
   return launch_row_ops<R, true>(a, nx, ny, s);
 }

@@ -26,7 +26,8 @@ EXPORTED = ('sgpe_version', 'sgpe_last_error', 'sgpe_plan_create',
             'sgpe_load_psik', 'sgpe_store_psik', 'sgpe_single_step',
             'sgpe_full_steps', 'sgpe_fft2', 'sgpe_time_passes',
             'sgpe_fft2_static', 'sgpe_set_energy_fields', 'sgpe_energy',
-            'sgpe_batch_create', 'sgpe_batch_destroy', 'sgpe_batch_steps')
+            'sgpe_batch_create', 'sgpe_batch_destroy', 'sgpe_batch_steps',
+            'sgpe_set_dft_mode')
 
 
 class SgpeError(RuntimeError):
@@ -84,6 +85,7 @@ _SIGS = {
                           ctypes.c_int),
     'sgpe_batch_destroy': ([_VP], ctypes.c_int),
     'sgpe_batch_steps': ([_VP, ctypes.c_int, _VP], ctypes.c_int),
+    'sgpe_set_dft_mode': ([_VP, ctypes.c_int], ctypes.c_int),
     'sgpe_fft2_static': ([ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP,
                           _VP, _VP, ctypes.c_int, ctypes.c_double, _VP],
                          ctypes.c_int),
@@ -155,6 +157,10 @@ class Plan:
             self.close()
         except Exception:   # interpreter shutdown
             pass
+
+    def set_dft_mode(self, mode):
+        """0: FP32 radix-16 DFTs; 1: split-BF16 tensor-core DFT16."""
+        check(load().sgpe_set_dft_mode(self._h, int(mode)))
 
     def set_physics(self, g_uu, g_dd, g_ud, atom_num, dv_r, dv_k,
                     is_coupling):

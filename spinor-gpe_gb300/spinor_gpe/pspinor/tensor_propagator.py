@@ -113,12 +113,15 @@ class TensorPropagator:
 
     Parameters follow ``tensor_propagator.py:67-91``: ``spin`` (a
     ``PSpinor``), ``t_step``, ``n_steps``, ``device``, ``time`` ('imag' or
-    'real'), ``is_sampling``, ``n_samples``; plus ``dtype`` (64 / 128).
+    'real'), ``is_sampling``, ``n_samples``; plus ``dtype`` (64 / 128) and
+    ``tensor_core_dft`` (complex64 only: radix-16 DFT stages as split-BF16
+    products on the tensor cores, a precision-study variant).
     """
 
     # pylint: disable=too-many-instance-attributes
     def __init__(self, spin, t_step, n_steps, device='cuda', time='imag',
-                 is_sampling=False, n_samples=1, dtype=128):
+                 is_sampling=False, n_samples=1, dtype=128,
+                 tensor_core_dft=False):
         self.n_steps = n_steps
         self._device = cuda_device(device)
         self.device = device
@@ -180,6 +183,9 @@ class TensorPropagator:
         self.sample_rate = self.n_steps / n_samples
 
         self._plan = _native.Plan(ny, nx, self._bits, self._device.index)
+        self.tensor_core_dft = bool(tensor_core_dft)
+        if self.tensor_core_dft:
+            self._plan.set_dft_mode(1)
         dv_r = float(self._space_np['dv_r'])
         dv_k = float(self._space_np['dv_k'])
         self._plan.set_physics(float(self.g_sc['uu']), float(self.g_sc['dd']),

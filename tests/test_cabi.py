@@ -48,6 +48,7 @@ def test_argument_errors_without_gpu(native_lib):
     assert lib.sgpe_set_physics(None, 1, 1, 1, 1, 1, 1, 0) == _native.SGPE_ERR_ARG
     assert lib.sgpe_full_steps(None, 1, None, None) == _native.SGPE_ERR_ARG
     assert lib.sgpe_plan_destroy(None) == _native.SGPE_OK
+    assert lib.sgpe_set_dft_mode(None, 1) == _native.SGPE_ERR_ARG
     with pytest.raises(_native.SgpeError):
         _native.check(lib.sgpe_single_step(None, 0, None))
     assert lib.sgpe_version() >= 100

@@ -451,3 +451,53 @@ def test_grouped_batch_matches_solves_alone(tp, tmp_path, monkeypatch, grouping)
         np.testing.assert_array_equal(np.array([t.cpu().numpy() for t in a.psik]),
                                       np.array([t.cpu().numpy() for t in b.psik]))
     batch.close()
+
+
+@pytest.mark.parametrize('shape', [(64, 256), (1024, 1024), (2048, 256)])
+def test_tensor_core_dft_fft_accuracy(shape):
+    """The split-BF16 tensor-core DFT16 transforms agree with NumPy to the
+    accuracy of the BF16 head/tail split (about 2^-16 per radix-16 stage),
+    and more loosely than the FP32 path."""
+    from spinor_gpe.pspinor import _native
+    rng = np.random.default_rng(3)
+    ny, nx = shape
+    a = [rng.standard_normal(shape) + 1j * rng.standard_normal(shape) for _ in range(2)]
+    t = [torch.as_tensor(x, dtype=torch.complex64, device='cuda') for x in a]
+    ref = [np.fft.fft2(x) for x in a]
+    errs = {}
+    for mode in (0, 1):
+        plan = _native.Plan(ny, nx, 64, 0)
+        plan.set_dft_mode(mode)
+        out = [torch.empty_like(x) for x in t]
+        plan.fft2(torch, t, out, 0, 1.0)
+        got = [np.fft.ifftshift(o.cpu().numpy()) for o in out]   # fft2 output is centred
+        errs[mode] = rel_l2(got, ref)
+    assert errs[0] <= 2e-6
+    assert 1e-7 < errs[1] <= 2e-4
+
+
+def test_tensor_core_dft_propagation_against_oracle(tp, tmp_path):
+    """A 256^2 complex64 imaginary-time run with tensor-core DFT16 stages
+    tracks the complex128 oracle within the BF16-split accuracy."""
+    from spinor_gpe import workloads
+    from spinor_gpe.pspinor import pspinor as spin
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    ps = workloads.ground_state_256(spin.PSpinor, ttools.fft_2d, str(tmp_path / 'tc') + '/')
+    steps = 20
+    ref, _ = _oracle_run(_inputs_from_spin(ps), 0.02, 'imag', steps)
+    res = {}
+    for tc in (False, True):
+        prop = tp.TensorPropagator(ps, 0.02, steps, 'cuda', time='imag', dtype=64,
+                                   tensor_core_dft=tc)
+        prop.full_steps(steps)
+        res[tc] = rel_l2(np.array([x.cpu().numpy() for x in prop.psik]), ref)
+    assert res[False] <= 1e-5
+    assert res[True] <= 2e-3
+    with pytest.raises(_native_error()):
+        tp.TensorPropagator(ps, 0.02, steps, 'cuda', time='imag', dtype=128,
+                            tensor_core_dft=True)
+
+
+def _native_error():
+    from spinor_gpe.pspinor import _native
+    return _native.SgpeError

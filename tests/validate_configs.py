@@ -13,8 +13,9 @@ solver's steps/s.
 * raman_quench_1024: 1024^2, complex64, 3000 imaginary steps at dt = 0.01,
   then delta 0 -> 0.5 and 10000 real steps at dt = 1e-3; real-time energy
   drift of both.
-* vortex_2048: 2048^2, complex64 (and complex128), 2000 imaginary steps at
-  dt = 0.01, 8 seeded vortices.
+* vortex_2048: 2048^2, complex64 with FP32 DFTs, complex64 with the
+  split-BF16 tensor-core DFT16 stages, and complex128; 2000 imaginary steps
+  at dt = 0.01, 8 seeded vortices.
 """
 import json
 import os
@@ -66,8 +67,9 @@ def rel_l2(a, b):
                  / np.linalg.norm(np.asarray(b).ravel()))
 
 
-def run_solver(ps, dt, n, time_mode, dtype):
-    prop = tprop.TensorPropagator(ps, dt, n, 'cuda', time=time_mode, dtype=dtype)
+def run_solver(ps, dt, n, time_mode, dtype, tensor_core_dft=False):
+    prop = tprop.TensorPropagator(ps, dt, n, 'cuda', time=time_mode, dtype=dtype,
+                                  tensor_core_dft=tensor_core_dft)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     prop.full_steps(n)
@@ -133,10 +135,11 @@ def vortex_2048(tmp):
     ps = workloads.vortex_2048(spin.PSpinor, ttools.fft_2d, tmp + '/c3/')
     ref = run_oracle(ps, 0.01, 2000, 'imag')
     ref64 = run_oracle(ps, 0.01, 2000, 'imag', 64)
-    for dtype in (64, 128):
-        _, mine, rate = run_solver(ps, 0.01, 2000, 'imag', dtype)
-        summary(f'vortex_2048 (complex{dtype}, 2000 imaginary steps)', ps, mine,
-                ref, rate, {'original_complex64_psik_rel_l2': rel_l2(ref64, ref)})
+    for dtype, tc in ((64, False), (64, True), (128, False)):
+        _, mine, rate = run_solver(ps, 0.01, 2000, 'imag', dtype, tc)
+        variant = 'split-BF16 tensor-core DFT16' if tc else 'FP32 DFT' if dtype == 64 else 'FP64'
+        summary(f'vortex_2048 (complex{dtype}, {variant}, 2000 imaginary steps)', ps,
+                mine, ref, rate, {'original_complex64_psik_rel_l2': rel_l2(ref64, ref)})
 
 
 CONFIGS = {'ground_state_256': ground_state_256,

@@ -102,6 +102,52 @@ template <int DIR, int M, class C> __device__ __forceinline__ C tw32(C a) {
   }
 }
 
+// multiply by exp(DIR * 2 pi i m / 24), m a compile-time constant
+template <int DIR, int M, class C> __device__ __forceinline__ C tw24(C a) {
+  using R = decltype(C::x);
+  constexpr int m = ((M % 24) + 24) % 24;
+  if constexpr (m == 0) {
+    return a;
+  } else if constexpr (m >= 6) {
+    return crot<DIR>(tw24<DIR, m - 6>(a));  // exp(DIR i pi/2) = DIR * i
+  } else {
+    // cos and sin of pi m / 12, m = 1..5
+    constexpr double kc[6] = {1.0, 0.96592582628906828675, 0.86602540378443864676, 0.70710678118654752440, 0.5,
+                              0.25881904510252076235};
+    const R d = R(DIR);
+    return cmul(a, cmake<C>(R(kc[m]), d * R(kc[6 - m])));  // sin(pi m/12) = cos(pi (6-m)/12)
+  }
+}
+// The same with the exponent known only after unrolling (the switch folds).
+template <int DIR, class C> __device__ __forceinline__ C tw24r(C a, int m) {
+  switch (((m % 24) + 24) % 24) {
+    case 0: return a;
+    case 1: return tw24<DIR, 1>(a);
+    case 2: return tw24<DIR, 2>(a);
+    case 3: return tw24<DIR, 3>(a);
+    case 4: return tw24<DIR, 4>(a);
+    case 5: return tw24<DIR, 5>(a);
+    case 6: return tw24<DIR, 6>(a);
+    case 7: return tw24<DIR, 7>(a);
+    case 8: return tw24<DIR, 8>(a);
+    case 9: return tw24<DIR, 9>(a);
+    case 10: return tw24<DIR, 10>(a);
+    case 11: return tw24<DIR, 11>(a);
+    case 12: return tw24<DIR, 12>(a);
+    case 13: return tw24<DIR, 13>(a);
+    case 14: return tw24<DIR, 14>(a);
+    case 15: return tw24<DIR, 15>(a);
+    case 16: return tw24<DIR, 16>(a);
+    case 17: return tw24<DIR, 17>(a);
+    case 18: return tw24<DIR, 18>(a);
+    case 19: return tw24<DIR, 19>(a);
+    case 20: return tw24<DIR, 20>(a);
+    case 21: return tw24<DIR, 21>(a);
+    case 22: return tw24<DIR, 22>(a);
+    default: return tw24<DIR, 23>(a);
+  }
+}
+
 // In-register DFT of size R in natural order: a[k] <- sum_n a[n] exp(DIR 2 pi i nk/R)
 template <int R, int DIR> struct Dft;
 
@@ -222,19 +268,52 @@ template <int DIR> struct Dft<32, DIR> {
   }
 };
 
-// Radix of the stage with sub-length NS of an (N, E) transform.  Powers of
-// two: E per stage, the remainder last.  N = 3 * 2^k: power-of-two stages of
-// at most P (the largest power of two dividing E), then one radix-3 stage.
+// DFT of size 3P (P = 4, 8): n = P n2 + n1, k = k1 + 3 k2; DFT3 over n2,
+// twiddle W_{3P}^{n1 k1}, DFT_P over n1.
+template <int P, int DIR> struct Dft3P {
+  template <class C> __device__ __forceinline__ static void run(C* a) {
+    constexpr int R = 3 * P;
+    constexpr int U = 24 / R;  // W_R^m = W_24^{U m}
+    C y[P][3];
+#pragma unroll
+    for (int n1 = 0; n1 < P; ++n1) {
+      C t[3] = {a[n1], a[P + n1], a[2 * P + n1]};
+      Dft<3, DIR>::run(t);
+      y[n1][0] = t[0];
+      y[n1][1] = tw24r<DIR>(t[1], U * n1);
+      y[n1][2] = tw24r<DIR>(t[2], U * 2 * n1);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < 3; ++k1) {
+      C u[P];
+#pragma unroll
+      for (int n1 = 0; n1 < P; ++n1) u[n1] = y[n1][k1];
+      Dft<P, DIR>::run(u);
+#pragma unroll
+      for (int k2 = 0; k2 < P; ++k2) a[k1 + 3 * k2] = u[k2];
+    }
+  }
+};
+template <int DIR> struct Dft<12, DIR> : Dft3P<4, DIR> {};
+template <int DIR> struct Dft<24, DIR> : Dft3P<8, DIR> {};
+
+// Radix of the stage with sub-length NS of an (N, E) transform.  With P the
+// largest power of two dividing E: powers of two take stages of P (the
+// remainder last).  N = 3 * 2^k with E a multiple of 3 dividing N (E = 24 or
+// 12): the first stage has radix E (an in-register DFT 3 x P), the rest are
+// powers of two, e.g. 768 = 24 x 8 x 4.  Otherwise N = 3 * 2^k takes
+// power-of-two stages of at most P and one radix-3 stage last.
 __host__ __device__ constexpr int stage_radix(int N, int E, int NS) {
   const int m = N / NS;
+  int p = 1;
+  while (E % (2 * p) == 0) p *= 2;
   if (m % 3 == 0) {
+    if (E % 3 == 0 && m % E == 0) return E;
     if (m == 3) return 3;
-    int p = 1;
-    while (E % (2 * p) == 0) p *= 2;
     const int two = m / 3;
     return two < p ? two : p;
   }
-  return m < E ? m : E;
+  return m < p ? m : p;
 }
 
 // Offset of the twiddle block of the stage with sub-length NS in the table

@@ -46,6 +46,13 @@ template <typename R> struct Tune;
 #ifndef SGPE_F32_R3_E
 #define SGPE_F32_R3_E 12
 #endif
+// ... for 768: 24 points per thread (768 = 24 x 8 x 4, three stages)
+#ifndef SGPE_F32_R3_E_LARGE
+#define SGPE_F32_R3_E_LARGE 24
+#endif
+#ifndef SGPE_F32_R3_COL_MINB_LARGE
+#define SGPE_F32_R3_COL_MINB_LARGE 2
+#endif
 #ifndef SGPE_F32_R3_ROW_MINB
 #define SGPE_F32_R3_ROW_MINB 4
 #endif
@@ -57,21 +64,23 @@ template <> struct Tune<float> {
   static constexpr int ROW_E_LARGE = SGPE_F32_ROW_E_LARGE, ROW_MINB_LARGE = SGPE_F32_ROW_MINB_LARGE;
   static constexpr int COL_E = SGPE_F32_COL_E, COLS = SGPE_F32_COLS, COL_MINB = SGPE_F32_COL_MINB;
   static constexpr int R3_E = SGPE_F32_R3_E, R3_ROW_MINB = SGPE_F32_R3_ROW_MINB, R3_COL_MINB = SGPE_F32_R3_COL_MINB;
+  static constexpr int R3_E_LARGE = SGPE_F32_R3_E_LARGE, R3_COL_MINB_LARGE = SGPE_F32_R3_COL_MINB_LARGE;
 };
 template <> struct Tune<double> {
   static constexpr int ROW_E = 8, ROW_THREADS = 256, ROW_MINB = 2;
   static constexpr int ROW_E_LARGE = 8, ROW_MINB_LARGE = 2;
   static constexpr int COL_E = 8, COLS = 4, COL_MINB = 1;
   static constexpr int R3_E = 12, R3_ROW_MINB = 2, R3_COL_MINB = 1;
+  static constexpr int R3_E_LARGE = 12, R3_COL_MINB_LARGE = 1;
 };
 
 constexpr int cmin(int a, int b) { return a < b ? a : b; }
 constexpr int cmax(int a, int b) { return a > b ? a : b; }
 
-// Points per thread: the tuned E for powers of two; Tune::R3_E for
-// N = 3 * 2^k, so that every stage radix divides it.
+// Points per thread: the tuned E for powers of two; Tune::R3_E (R3_E_LARGE
+// from 768) for N = 3 * 2^k, multiples of 3 dividing N.
 template <typename R> constexpr int pick_e(int n, int e_pow2) {
-  return (n % 3 == 0) ? Tune<R>::R3_E : cmin(n, e_pow2);
+  return (n % 3 == 0) ? (n >= 768 ? Tune<R>::R3_E_LARGE : Tune<R>::R3_E) : cmin(n, e_pow2);
 }
 
 template <typename R, int N> struct RowCfg {
@@ -92,8 +101,9 @@ template <typename R, int N> struct ColCfg {
   static constexpr int COLS = cmax(cmin(Tune<R>::COLS, 1024 / T), 32 / T);
   static constexpr int THREADS = T * COLS;
   static constexpr size_t SMEM = size_t(COLS) * (N + N / E + 2) * sizeof(Cx<R>);
-  static constexpr int MINB =
-      cmax(1, cmin(N % 3 == 0 ? Tune<R>::R3_COL_MINB : Tune<R>::COL_MINB, 1024 / THREADS));
+  static constexpr int MINB = cmax(
+      1, cmin(N % 3 == 0 ? (N >= 768 ? Tune<R>::R3_COL_MINB_LARGE : Tune<R>::R3_COL_MINB) : Tune<R>::COL_MINB,
+              1024 / THREADS));
 };
 
 // Supported line lengths: powers of two 32..4096 and 3 * 2^k for 192, 384, 768.

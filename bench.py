@@ -62,6 +62,9 @@ def parse():
                          'request stream through the continuous-batching loop '
                          'against the same requests solved one after another)')
     ap.add_argument('--solves', type=int, default=96)
+    ap.add_argument('--breakdown', action='store_true',
+                    help='batched_uneven: also time each grid-size class alone '
+                         '(one solve, the class sequentially, the class batched)')
     ap.add_argument('--batch-steps', type=int, default=2000)
     ap.add_argument('--serve-rate', type=float, default=200.0)
     ap.add_argument('--serve-window', type=float, default=0.5)
@@ -414,6 +417,21 @@ def run_batched(args, world, rank, local):
         p.full_steps(max(args.warmup, 9))
     t_seq = timed(lambda: [p.full_steps(k) for p in props])
 
+    breakdown = None
+    if args.breakdown:
+        breakdown = {}
+        kb = max(20, k // 10)
+        for n in sorted({s.psik[0].shape[0] for s in spins}):
+            cls = [p for p, s in zip(props, spins) if s.psik[0].shape[0] == n]
+            t_one = timed(lambda: cls[0].full_steps(kb)) / kb
+            cb = PropagatorBatch(cls)
+            cb.full_steps(9)
+            t_grp = timed(lambda: cb.full_steps(kb)) / kb
+            cb.close()
+            breakdown[str(n)] = {'solves': len(cls), 'one_alone_us': 1e6 * t_one,
+                                 'sequential_us': 1e6 * t_one * len(cls),
+                                 'batched_us': 1e6 * t_grp}
+
     batch = PropagatorBatch(props)
     batch.full_steps(max(args.warmup, 9))
     with ClockSampler(local) as clk:
@@ -445,6 +463,7 @@ def run_batched(args, world, rank, local):
                                      'with TensorPropagator.full_steps'},
         'speedup_vs_sequential': value / seq,
         'gpu_launches': 6 * k * args.solves,
+        'per_class_step_us': breakdown,
         'clocks': clk.summary(),
     }
     batch.close()

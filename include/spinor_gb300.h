@@ -164,6 +164,18 @@ int sgpe_set_energy_fields(sgpe_plan* plan, int slot, const sgpe_energy_fields* 
  * spectral instead of finite differences of the unwrapped phase. */
 int sgpe_energy(sgpe_plan* plan, int slot, const void* psik0, const void* psik1, double* out_dev, void* stream);
 
+/* Post-analysis of a final spinor (the derived fields of the original's
+ * PropResult, spinor_gpe/pspinor/prop_result.py:76-88), all device pointers
+ * of the plan's grid and precision:
+ *   dens_c = |psi_c|^2, densk_c = |psik_c|^2 (real, working precision),
+ *   phase_c = angle(psi_c), 0 where dens_c < 1e-6 max dens_c
+ *             (tensor_tools.py:514-539 without unwrapping),
+ *   sums_dev[5] = [sum n0 n1, sum n0^2, sum n1^2, max n0, max n1] (FP64),
+ * from which calc_separation = 1 - s0 / sqrt(s1 s2). */
+int sgpe_analysis(sgpe_plan* plan, const void* psi0, const void* psi1, const void* psik0, const void* psik1,
+                  void* dens0, void* dens1, void* densk0, void* densk1, void* phase0, void* phase1,
+                  double* sums_dev, void* stream);
+
 /* Measurement helper: n_steps full steps exactly as sgpe_full_steps (no
  * populations), captured into a CUDA graph with events around every column
  * pass and every row pass, launched once on `stream`.  Synchronises the

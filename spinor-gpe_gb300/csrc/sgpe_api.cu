@@ -16,6 +16,7 @@
 #include <string>
 #include <vector>
 
+#include "sgpe_analysis.cuh"
 #include "sgpe_energy.cuh"
 #include "sgpe_launch.cuh"
 #include "spinor_gb300.h"
@@ -133,6 +134,7 @@ struct sgpe_plan {
   EnergyFields efield[2];
   void* epsi[2] = {nullptr, nullptr};   // real-space spinor for the energy
   double* epart = nullptr;              // energy block partials [2][kEnergyBlocks][6]
+  double* apart = nullptr;              // analysis block partials
   double g[3] = {0, 0, 0};
   double atom_num = 1.0, dv_r = 1.0, dv_k = 1.0;
   int coupling = 0;
@@ -839,6 +841,7 @@ int sgpe_plan_destroy(sgpe_plan* p) {
     if (p->epsi[c]) cudaFree(p->epsi[c]);
   if (p->epart) cudaFree(p->epart);
   if (p->tcb) cudaFree(p->tcb);
+  if (p->apart) cudaFree(p->apart);
   delete p;
   return SGPE_OK;
 }
@@ -1082,6 +1085,51 @@ int sgpe_energy(sgpe_plan* p, int slot, const void* k0, const void* k1, double* 
   DeviceGuard g(p->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   return p->bits == 64 ? energy_impl<float>(p, slot, k0, k1, out, s) : energy_impl<double>(p, slot, k0, k1, out, s);
+}
+
+}  // extern "C"
+
+namespace {
+template <typename R>
+int analysis_impl(sgpe_plan* p, const void* const* in, void* const* out, double* sums, cudaStream_t s) {
+  using C = sgpe::Cx<R>;
+  sgpe::AnalysisArgs<R> a{};
+  for (int c = 0; c < 2; ++c) {
+    a.psi[c] = static_cast<const C*>(in[c]);
+    a.psik[c] = static_cast<const C*>(in[2 + c]);
+    a.dens[c] = static_cast<R*>(out[c]);
+    a.densk[c] = static_cast<R*>(out[2 + c]);
+    a.phase[c] = static_cast<R*>(out[4 + c]);
+  }
+  a.n = (long long)p->nx * p->ny;
+  a.part = p->apart;
+  a.sums = sums;
+  sgpe::analysis_dens_kernel<R><<<sgpe::kAnalysisBlocks, 256, 0, s>>>(a);
+  sgpe::analysis_finalize_kernel<<<1, 32, 0, s>>>(p->apart, sgpe::kAnalysisBlocks, sums);
+  sgpe::analysis_phase_kernel<R><<<sgpe::kAnalysisBlocks, 256, 0, s>>>(a);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? SGPE_OK : cuda_fail(e, "analysis");
+}
+}  // namespace
+
+extern "C" {
+
+int sgpe_analysis(sgpe_plan* p, const void* psi0, const void* psi1, const void* psik0, const void* psik1,
+                  void* dens0, void* dens1, void* densk0, void* densk1, void* phase0, void* phase1,
+                  double* sums_dev, void* stream) {
+  if (p == nullptr || !psi0 || !psi1 || !psik0 || !psik1 || !dens0 || !dens1 || !densk0 || !densk1 || !phase0 ||
+      !phase1 || !sums_dev)
+    return fail(SGPE_ERR_ARG, "null plan or data pointer");
+  DeviceGuard g(p->device);
+  if (p->apart == nullptr) {
+    const cudaError_t e =
+        cudaMalloc(reinterpret_cast<void**>(&p->apart), sizeof(double) * sgpe::kAnalysisBlocks * sgpe::kAnalysisSums);
+    if (e != cudaSuccess) return fail(SGPE_ERR_OOM, std::string("analysis partials: ") + cudaGetErrorString(e));
+  }
+  const void* in[4] = {psi0, psi1, psik0, psik1};
+  void* out[6] = {dens0, dens1, densk0, densk1, phase0, phase1};
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return p->bits == 64 ? analysis_impl<float>(p, in, out, sums_dev, s) : analysis_impl<double>(p, in, out, sums_dev, s);
 }
 
 int sgpe_time_passes(sgpe_plan* p, int n_steps, double* col_ms, double* row_ms, void* stream) {

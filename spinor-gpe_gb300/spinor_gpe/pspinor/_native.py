@@ -27,7 +27,7 @@ EXPORTED = ('sgpe_version', 'sgpe_last_error', 'sgpe_plan_create',
             'sgpe_full_steps', 'sgpe_fft2', 'sgpe_time_passes',
             'sgpe_fft2_static', 'sgpe_set_energy_fields', 'sgpe_energy',
             'sgpe_batch_create', 'sgpe_batch_destroy', 'sgpe_batch_steps',
-            'sgpe_set_dft_mode')
+            'sgpe_set_dft_mode', 'sgpe_analysis')
 
 
 class SgpeError(RuntimeError):
@@ -86,6 +86,7 @@ _SIGS = {
     'sgpe_batch_destroy': ([_VP], ctypes.c_int),
     'sgpe_batch_steps': ([_VP, ctypes.c_int, _VP], ctypes.c_int),
     'sgpe_set_dft_mode': ([_VP, ctypes.c_int], ctypes.c_int),
+    'sgpe_analysis': ([_VP] + [_VP] * 10 + [_VP, _VP], ctypes.c_int),
     'sgpe_fft2_static': ([ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP,
                           _VP, _VP, ctypes.c_int, ctypes.c_double, _VP],
                          ctypes.c_int),
@@ -241,6 +242,14 @@ class Plan:
         device)."""
         check(load().sgpe_energy(self._h, int(slot), _ptr(psik[0]), _ptr(psik[1]),
                                  _ptr(out), _stream(torch, psik[0].device)))
+
+    def analysis(self, torch, psi, psik, dens, densk, phase, sums):
+        """Densities, masked phases and FP64 separation sums (device)."""
+        check(load().sgpe_analysis(
+            self._h, _ptr(psi[0]), _ptr(psi[1]), _ptr(psik[0]), _ptr(psik[1]),
+            _ptr(dens[0]), _ptr(dens[1]), _ptr(densk[0]), _ptr(densk[1]),
+            _ptr(phase[0]), _ptr(phase[1]), _ptr(sums),
+            _stream(torch, psi[0].device)))
 
     def fft2(self, torch, inp, out, inverse, scale):
         check(load().sgpe_fft2(self._h, _ptr(inp[0]), _ptr(inp[1]),

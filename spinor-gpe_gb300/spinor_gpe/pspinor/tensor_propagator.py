@@ -319,9 +319,39 @@ class TensorPropagator:
         else:
             file_name = None
 
+        psi_t = ttools.ifft_2d(psik_t, self._space_np['dr'])
+        derived = {k: (ttools.to_numpy(v) if isinstance(v, list) else v)
+                   for k, v in self.analysis(psi_t, psik_t).items()}
         psik = ttools.to_numpy(psik_t)
-        psi = ttools.to_numpy(ttools.ifft_2d(psik_t, self._space_np['dr']))
-        return prop_result.PropResult(psi, psik, energy, pops, file_name)
+        psi = ttools.to_numpy(psi_t)
+        return prop_result.PropResult(psi, psik, energy, pops, file_name,
+                                      derived=derived)
+
+    def analysis(self, psi=None, psik=None):
+        """Derived fields of a spinor computed on the device (the
+        original's ``PropResult`` fields, prop_result.py:76-88): component
+        densities ``dens``, k-space densities ``densk``, phases ``phase``
+        (zero where the density is below 1e-6 of its maximum), and ``sums``
+        = [sum n0 n1, sum n0^2, sum n1^2, max n0, max n1] in FP64 with
+        ``separation`` = 1 - sums[0] / sqrt(sums[1] sums[2]).  Defaults:
+        the current state."""
+        if psik is None:
+            psik = self.psik
+        if psi is None:
+            psi = ttools.ifft_2d(psik, self._space_np['dr'])
+        psi = [torch.as_tensor(p, device=self._device).to(self._ctype).contiguous()
+               for p in psi]
+        psik = [torch.as_tensor(p, device=self._device).to(self._ctype).contiguous()
+                for p in psik]
+        def empty():
+            return [torch.empty(self._shape, dtype=self._rtype, device=self._device)
+                    for _ in range(2)]
+        dens, densk, phase = empty(), empty(), empty()
+        sums = torch.empty(5, dtype=torch.float64, device=self._device)
+        self._plan.analysis(torch, psi, psik, dens, densk, phase, sums)
+        s = sums.cpu().numpy()
+        return {'dens': dens, 'densk': densk, 'phase': phase, 'sums': s,
+                'separation': float(1 - s[0] / np.sqrt(s[1] * s[2]))}
 
     # --------------------------------------------------------------- energy
     ENERGY_KEYS = ('kin', 'pot', 'int', 'cpl', 'total', 'mu', 'atoms_k',

@@ -501,3 +501,34 @@ def test_tensor_core_dft_propagation_against_oracle(tp, tmp_path):
 def _native_error():
     from spinor_gpe.pspinor import _native
     return _native.SgpeError
+
+
+@pytest.mark.parametrize('dtype', [64, 128])
+def test_device_analysis_matches_numpy(tp, tmp_path, dtype):
+    """Densities, masked phases and the separation measure of PropResult
+    computed on the device agree with the NumPy formulas of the original."""
+    from spinor_gpe import workloads
+    from spinor_gpe.pspinor import pspinor as spin
+    from spinor_gpe.pspinor import prop_result
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    ps = workloads.build(spin.PSpinor, ttools.fft_2d, str(tmp_path / 'an') + '/',
+                         nx=128, ny=64, half_x=8.0, half_y=4.0, g=(500.0, 490.0, 480.0),
+                         omega=0.9, k_l=2.0, delta=0.2, seed=31)
+    prop = tp.TensorPropagator(ps, 0.02, 10, 'cuda', time='imag', dtype=dtype)
+    prop.full_steps(10)
+    d = prop.analysis()
+    psik = ttools.to_numpy(prop.psik)
+    psi = ttools.to_numpy(ttools.ifft_2d(prop.psik, ps.space['dr']))
+    ref = prop_result.PropResult(psi, psik, 0.0, {})
+    tol = 1e-6 if dtype == 64 else 1e-13
+    for c in range(2):
+        assert rel_l2(d['dens'][c].cpu().numpy(), ref.dens[c]) <= tol
+        assert rel_l2(d['densk'][c].cpu().numpy(), ref.densk[c]) <= tol
+        got_ph = d['phase'][c].cpu().numpy()
+        # equal away from the mask edge and the +-pi branch cut
+        ok = np.isclose(got_ph, ref.phase[c], rtol=0, atol=1e-5) | \
+            np.isclose(np.abs(got_ph - ref.phase[c]), 2 * np.pi, atol=1e-5)
+        assert ok.mean() > 0.999
+    assert abs(d['separation'] - ref.calc_separation()) <= 1e-6
+    res = prop.prop_loop(5)
+    assert abs(res.calc_separation() - prop.analysis()['separation']) <= 1e-12

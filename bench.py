@@ -69,6 +69,9 @@ def parse():
     ap.add_argument('--serve-rate', type=float, default=200.0)
     ap.add_argument('--serve-window', type=float, default=0.5)
     ap.add_argument('--max-active', type=int, default=64)
+    ap.add_argument('--host-setup', action='store_true',
+                    help='served: build each request with the host PSpinor '
+                         'set-up instead of the device set-up')
     return ap.parse_args()
 
 
@@ -477,8 +480,9 @@ def run_served(args, world, rank, local):
     """A seeded Poisson request stream (70% ground states at 256^2/512^2 run
     to |dE| < 1e-8 per step or 3000 steps, 30% real-time quenches at 1024^2
     for 5000 steps; complex64) served by the continuous-batching loop under
-    a 150 GB admission cap, then the same requests solved one after another
-    by the plain drop-in.  Reports latency percentiles (arrival to result),
+    a 150 GB admission cap (requests set up on the device unless
+    --host-setup), then the same requests solved one after another by the
+    plain drop-in.  Reports latency percentiles (arrival to result),
     offered and served load, aggregate grid-point-steps/s of both."""
     import torch
     from spinor_gpe import serve, workloads
@@ -487,7 +491,8 @@ def run_served(args, world, rank, local):
     tmp = tempfile.mkdtemp(prefix='sgpe_serve_')
     stream = workloads.served_stream(rate=args.serve_rate,
                                      window=args.serve_window, seed=5 + rank)
-    reqs = serve.requests_from_stream(stream, tmp + '/', device=device)
+    reqs = serve.requests_from_stream(stream, tmp + '/', device=device,
+                                      device_setup=not args.host_setup)
     offered_max = sum(r.max_steps * r.grid_points for r in reqs)
     # warm-up: one small solve through the loop (library load, first graphs)
     serve.SolveServer(device, max_active=2).run(reqs[:1], realtime=False)
@@ -530,6 +535,8 @@ def run_served(args, world, rank, local):
                    'requests': len(res), 'rate_per_s': args.serve_rate,
                    'window_s': args.serve_window, 'hbm_cap_bytes': 150e9,
                    'max_active': args.max_active,
+                   'setup': 'host PSpinor' if args.host_setup else
+                            'DeviceSpinor (set-up kernels on the GPU)',
                    'parallelism': f'replicas x{world}'},
         'offered': {'requests_per_s': args.serve_rate,
                     'grid_point_steps_upper_bound': offered_max,

@@ -176,6 +176,34 @@ int sgpe_analysis(sgpe_plan* plan, const void* psi0, const void* psi1, const voi
                   void* dens0, void* dens1, void* densk0, void* densk1, void* phase0, void* phase1,
                   double* sums_dev, void* stream);
 
+/* Initial-state set-up on the device for a separable trap V = vx(x) + vy(y)
+ * (the O(Nx Ny) parts of the original's PSpinor set-up,
+ * spinor_gpe/pspinor/pspinor.py:248-281): writes the Thomas-Fermi spinor
+ *   psi_c = sqrt(max(mu - V, 0)) * amp_c * exp(i phi_c)
+ * (amp: 2 complex values as (re, im) pairs; phi_c ~ U(-noise, noise) from a
+ * counter-based hash of (seed, component, point); noise = 0: none) to
+ * psi0/psi1 (complex64 or complex128, (ny, nx) row-major), then, if
+ * atom_num > 0, renormalises to atom_num with volume element dv_r.
+ * vx (nx), vy (ny) are FP64 device arrays; scratch holds 304 doubles. */
+int sgpe_setup_spinor(int dtype_bits, int ny, int nx, const double* vx, const double* vy, double mu,
+                      const double* amp, double noise, unsigned long long seed, double atom_num, double dv_r,
+                      double* scratch, void* psi0, void* psi1, void* stream);
+
+/* psi_c *= prod_j f(r_j / heal_c) exp(i w_j atan2(y - y_j, x - x_j)),
+ * f(g) = g / sqrt(g^2 + 1), for the vortices vort[j] = (component, x_j, y_j,
+ * w_j) (FP64 device array of n_vort x 4); x (nx), y (ny) the grid coordinates
+ * (device), heal[2] host values.  Replaces seed_vortices
+ * (spinor_gpe/pspinor/pspinor.py:680-745). */
+int sgpe_imprint_vortices(int dtype_bits, int ny, int nx, const double* x, const double* y, const double* vort,
+                          int n_vort, const double* heal, void* psi0, void* psi1, void* stream);
+
+/* out = f_plus S(+shift) in + f_minus S(-shift) in for one (ny, nx)
+ * component, S(s) the multiplication by exp(-2 pi i s fftfreq(nx)[ix]) along
+ * x: the momentum split of shift_momentum (spinor_gpe/pspinor/pspinor.py:
+ * 503-545, scipy.ndimage.fourier_shift of the centred transform). */
+int sgpe_fourier_split_x(int dtype_bits, int ny, int nx, double shift, double f_plus, double f_minus,
+                         const void* in, void* out, void* stream);
+
 /* Measurement helper: n_steps full steps exactly as sgpe_full_steps (no
  * populations), captured into a CUDA graph with events around every column
  * pass and every row pass, launched once on `stream`.  Synchronises the

@@ -27,7 +27,8 @@ EXPORTED = ('sgpe_version', 'sgpe_last_error', 'sgpe_plan_create',
             'sgpe_full_steps', 'sgpe_fft2', 'sgpe_time_passes',
             'sgpe_fft2_static', 'sgpe_set_energy_fields', 'sgpe_energy',
             'sgpe_batch_create', 'sgpe_batch_destroy', 'sgpe_batch_steps',
-            'sgpe_set_dft_mode', 'sgpe_analysis')
+            'sgpe_set_dft_mode', 'sgpe_analysis', 'sgpe_setup_spinor',
+            'sgpe_imprint_vortices', 'sgpe_fourier_split_x')
 
 
 class SgpeError(RuntimeError):
@@ -87,6 +88,15 @@ _SIGS = {
     'sgpe_batch_steps': ([_VP, ctypes.c_int, _VP], ctypes.c_int),
     'sgpe_set_dft_mode': ([_VP, ctypes.c_int], ctypes.c_int),
     'sgpe_analysis': ([_VP] + [_VP] * 10 + [_VP, _VP], ctypes.c_int),
+    'sgpe_setup_spinor': ([ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP,
+                           ctypes.c_double, _VP, ctypes.c_double, ctypes.c_ulonglong,
+                           ctypes.c_double, ctypes.c_double, _VP, _VP, _VP, _VP],
+                          ctypes.c_int),
+    'sgpe_imprint_vortices': ([ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP,
+                               _VP, ctypes.c_int, _VP, _VP, _VP, _VP], ctypes.c_int),
+    'sgpe_fourier_split_x': ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                              ctypes.c_double, ctypes.c_double, _VP, _VP, _VP],
+                             ctypes.c_int),
     'sgpe_fft2_static': ([ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP,
                           _VP, _VP, ctypes.c_int, ctypes.c_double, _VP],
                          ctypes.c_int),
@@ -121,6 +131,10 @@ def check(code):
 
 def _ptr(t):
     return ctypes.c_void_p(t.data_ptr())
+
+
+c_ptr = _ptr
+c_void_p = ctypes.c_void_p
 
 
 def _stream(torch, device):

@@ -22,6 +22,88 @@ from dataclasses import dataclass, field
 import numpy as np
 
 
+class SepField:
+    """A real FP64 field on the (Ny, Nx) grid kept as two 1-D parts,
+    value[y, x] = a[x] + b[y]: the separable energy grids and axis-aligned
+    coupling/detuning fields of a device-built spinor, which never need the
+    full 2-D array on the host.  ``np.asarray`` materialises it."""
+    __array_priority__ = 100
+
+    def __init__(self, a, b):
+        self.a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+        self.b = np.ascontiguousarray(b, dtype=np.float64).ravel()
+
+    @property
+    def shape(self):
+        return (self.b.size, self.a.size)
+
+    def __array__(self, dtype=None, copy=None):
+        arr = self.b[:, None] + self.a[None, :]
+        return arr if dtype is None else arr.astype(dtype)
+
+    def min(self):
+        return float(self.a.min() + self.b.min())
+
+    def max(self):
+        return float(self.a.max() + self.b.max())
+
+    def __add__(self, o):
+        if isinstance(o, SepField):
+            return SepField(self.a + o.a, self.b + o.b)
+        return SepField(self.a + float(o), self.b)
+
+    __radd__ = __add__
+
+    def __sub__(self, o):
+        if isinstance(o, SepField):
+            return SepField(self.a - o.a, self.b - o.b)
+        return SepField(self.a - float(o), self.b)
+
+    def __rsub__(self, o):
+        return SepField(float(o) - self.a, -self.b)
+
+    def __neg__(self):
+        return SepField(-self.a, -self.b)
+
+    def __mul__(self, o):
+        return SepField(self.a * float(o), self.b * float(o))
+
+    __rmul__ = __mul__
+
+    def __truediv__(self, o):
+        return SepField(self.a / float(o), self.b / float(o))
+
+    def __pow__(self, k):
+        if np.all(self.b == 0):
+            return SepField(self.a ** k, self.b)
+        if np.all(self.a == 0):
+            return SepField(self.a, self.b ** k)
+        raise ValueError('a power of a field varying along both axes is not separable')
+
+    def kind(self):
+        """'uniform', 'x', 'y' or 'sep'."""
+        a_const = bool(np.all(self.a == self.a[0]))
+        b_const = bool(np.all(self.b == self.b[0]))
+        if a_const and b_const:
+            return 'uniform'
+        if b_const:
+            return 'x'
+        if a_const:
+            return 'y'
+        return 'sep'
+
+    def profile(self):
+        """(kind, values) as _axes_profile gives for the materialised field."""
+        k = self.kind()
+        if k == 'uniform':
+            return k, np.array([self.a[0] + self.b[0]])
+        if k == 'x':
+            return k, self.a + self.b[0]
+        if k == 'y':
+            return k, self.b + self.a[0]
+        return None, None
+
+
 @dataclass
 class FieldSpec:
     """Complex values with broadcast strides: value(x, y) = values[x*sx + y*sy]."""
@@ -94,6 +176,14 @@ class Decomposition:
     (split_separable), or 'full' with the field itself."""
 
     def __init__(self, energy):
+        if isinstance(energy, SepField):
+            self.shape = energy.shape
+            kind, vals = energy.profile()
+            if kind is not None:
+                self.kind, self.vals = kind, vals
+            else:
+                self.kind, self.vals = 'sep', (energy.a.copy(), energy.b.copy())
+            return
         e = np.asarray(energy, dtype=np.float64)
         self.shape = e.shape
         kind, vals = _axes_profile(e)
@@ -140,6 +230,13 @@ class Compressed:
     gives."""
 
     def __init__(self, values):
+        if isinstance(values, SepField):
+            self.nx = values.shape[1]
+            kind, vals = values.profile()
+            if kind is not None:
+                self.kind, self.vals = kind, vals
+                return
+            values = np.asarray(values)
         v = np.asarray(values)
         self.nx = v.shape[1]
         kind, vals = _axes_profile(v)
@@ -171,7 +268,31 @@ def energy_pair(energy):
 
 def natural_order(k_field):
     """Centred (fftshift) k-space field -> natural FFT order."""
+    if isinstance(k_field, SepField):
+        return SepField(np.fft.ifftshift(k_field.a), np.fft.ifftshift(k_field.b))
     return np.fft.ifftshift(np.asarray(k_field))
+
+
+def as_field(v):
+    """A separable field as it is, anything else as an FP64 array."""
+    return v if isinstance(v, SepField) else np.asarray(v, dtype=np.float64)
+
+
+def coupling_energy_spec(coupling, theta, nx):
+    """The coupling-energy field (Omega/2) exp(-i theta) as one spec
+    (theta = None: no Raman phase), element for element what
+    value_op(coupling / 2 * exp(-i theta)) gives, without forming 2-D arrays
+    when both factors are constant along an axis."""
+    cc = Compressed(coupling)
+    if theta is None:
+        return cc.apply(lambda w: w / 2 + 0j)
+    th = Compressed(theta)
+    kinds = {cc.kind, th.kind}
+    if kinds <= {'uniform', 'x'} or kinds <= {'uniform', 'y'}:
+        kind = 'uniform' if kinds == {'uniform'} else (kinds - {'uniform'}).pop()
+        vals = np.asarray(cc.vals / 2 * np.exp(-1.0j * th.vals), dtype=np.complex128)
+        return _spec(vals, kind, nx)
+    return value_op(np.asarray(coupling) / 2 * np.exp(-1.0j * np.asarray(theta)), nx)
 
 
 class Prepared:
@@ -182,18 +303,23 @@ class Prepared:
     def __init__(self, kin_eng_spin, pot_eng_spin, coupling, expon):
         self.kin = self.decompose([natural_order(k) for k in kin_eng_spin])
         self.pot = self.decompose(pot_eng_spin)
-        self.coupling = Compressed(np.asarray(coupling, dtype=np.float64))
-        self.expon = (None if expon is None else
-                      Compressed(np.asarray(expon, dtype=np.float64)))
+        self.coupling = Compressed(as_field(coupling))
+        self.expon = (None if expon is None else Compressed(as_field(expon)))
 
     @staticmethod
     def decompose(fields):
         """Decompositions of two component fields (one shared when equal)."""
-        f = [np.asarray(x, dtype=np.float64) for x in fields]
+        f = [as_field(x) for x in fields]
         d0 = Decomposition(f[0])
-        if f[1] is f[0] or np.array_equal(f[1], f[0]):
+        if f[1] is f[0]:
             return [d0, d0]
-        return [d0, Decomposition(f[1])]
+        if isinstance(f[0], SepField) and isinstance(f[1], SepField):
+            same = np.array_equal(f[0].a, f[1].a) and np.array_equal(f[0].b, f[1].b)
+        elif isinstance(f[0], SepField) or isinstance(f[1], SepField):
+            same = False
+        else:
+            same = np.array_equal(f[1], f[0])
+        return [d0, d0] if same else [d0, Decomposition(f[1])]
 
 
 def build_substep(t_sub, kin_eng_spin, pot_eng_spin, coupling, expon, outer,

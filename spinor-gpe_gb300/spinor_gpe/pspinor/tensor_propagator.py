@@ -63,6 +63,11 @@ def cuda_device(device):
     return dev
 
 
+def _space_value(v):
+    """A grid quantity: separable meshes as they are, the rest as arrays."""
+    return v if isinstance(v, ops.SepField) else np.asarray(v)
+
+
 class SubstepOperators(dict):
     """``eng_out`` / ``eng_in``: the operators of one sub-step.
 
@@ -149,32 +154,30 @@ class TensorPropagator:
         self._ctype = torch.complex64 if self._bits == 64 else torch.complex128
         self._rtype = torch.float32 if self._bits == 64 else torch.float64
 
-        self._kin_np = [np.asarray(k, dtype=np.float64)
-                        for k in spin.kin_eng_spin]
-        self._pot_np = [np.asarray(v, dtype=np.float64)
-                        for v in spin.pot_eng_spin]
-        self._coupling_np = np.asarray(spin.coupling, dtype=np.float64)
-        psik0 = [np.asarray(p) for p in spin.psik]
-        self._shape = psik0[0].shape
+        # FP64 fields; separable fields of a device-built spinor stay as
+        # their 1-D parts (ops.SepField) and are never formed in 2-D here
+        self._kin_np = [ops.as_field(k) for k in spin.kin_eng_spin]
+        self._pot_np = [ops.as_field(v) for v in spin.pot_eng_spin]
+        self._coupling_np = ops.as_field(spin.coupling)
+        psik0 = [p if isinstance(p, torch.Tensor) else np.asarray(p)
+                 for p in spin.psik]
+        self._shape = tuple(psik0[0].shape)
         ny, nx = self._shape
         keys_space = ['dr', 'dk', 'x_mesh', 'y_mesh', 'dv_r', 'dv_k']
-        self._space_np = {k: np.asarray(spin.space[k]) for k in keys_space}
-        self._kx_np = np.asarray(spin.space['kx_mesh']) \
+        self._space_np = {k: _space_value(spin.space[k]) for k in keys_space}
+        self._kx_np = _space_value(spin.space['kx_mesh']) \
             if 'kx_mesh' in spin.space else None
-        self._ky_np = np.asarray(spin.space['ky_mesh']) \
+        self._ky_np = _space_value(spin.space['ky_mesh']) \
             if 'ky_mesh' in spin.space else None
-        self.space = {k: torch.tensor(v, device=self._device)
-                      for k, v in self._space_np.items()}
+        self._space_dev = None
 
         # pylint: disable=invalid-name
         self.kL_recoil = spin.kL_recoil
         self.rot_coupling = spin.rot_coupling
         if spin.rot_coupling:                     # tensor_propagator.py:125-129
             self._expon_np = None
-            self.expon = torch.tensor(0.0)
         else:
             self._expon_np = 2 * self.kL_recoil * self._space_np['x_mesh']
-            self.expon = torch.as_tensor(self._expon_np, device=self._device)
 
         if self.is_sampling:
             assert self.n_steps % n_samples == 0, (
@@ -210,18 +213,36 @@ class TensorPropagator:
 
     # ------------------------------------------------------------ attributes
     @property
+    def space(self):
+        """Grid quantities as device tensors (tensor_propagator.py:118-121),
+        formed on first access."""
+        if self._space_dev is None:
+            self._space_dev = {k: torch.tensor(np.asarray(v), device=self._device)
+                               for k, v in self._space_np.items()}
+        return self._space_dev
+
+    @property
+    def expon(self):
+        """The Raman phase 2 kL x as a device tensor (0 in the rotated frame)."""
+        if self._expon_np is None:
+            return torch.tensor(0.0)
+        return torch.as_tensor(np.asarray(self._expon_np), device=self._device)
+
+    @property
     def kin_eng_spin(self):
         """Kinetic energy grids as device tensors (tensor_propagator.py:114)."""
-        return [torch.as_tensor(k, device=self._device) for k in self._kin_np]
+        return [torch.as_tensor(np.asarray(k), device=self._device)
+                for k in self._kin_np]
 
     @property
     def pot_eng_spin(self):
         """Potential energy grids as device tensors (tensor_propagator.py:116)."""
-        return [torch.as_tensor(v, device=self._device) for v in self._pot_np]
+        return [torch.as_tensor(np.asarray(v), device=self._device)
+                for v in self._pot_np]
 
     @property
     def coupling(self):
-        return torch.as_tensor(self._coupling_np, device=self._device)
+        return torch.as_tensor(np.asarray(self._coupling_np), device=self._device)
 
     @property
     def psik(self):
@@ -365,16 +386,15 @@ class TensorPropagator:
         kin0 = [ops.energy_pair(d)
                 for d in ops.Prepared.decompose(self._kin_np)]
         pot = [ops.energy_pair(d) for d in self._prepared.pot]
-        theta = 0.0 if self._expon_np is None else self._expon_np
         nx = self._shape[1]
-        cpl0 = ops.value_op(self._coupling_np / 2 * np.exp(-1.0j * theta), nx)
+        cpl0 = ops.coupling_energy_spec(self._coupling_np, self._expon_np, nx)
         self._plan.set_energy_fields(0, kin0, pot, cpl0)
         if self._kx_np is not None and self._ky_np is not None:
             k_ref = (self._kx_np**2 + self._ky_np**2) / 2
             if self.is_coupling:
                 k_ref = k_ref + self.kL_recoil * self._kx_np
-            kin1 = [ops.energy_pair(k_ref)] * 2
-            cpl1 = ops.value_op(self._coupling_np / 2 + 0j, nx)
+            kin1 = [ops.energy_pair(ops.Decomposition(k_ref))] * 2
+            cpl1 = ops.coupling_energy_spec(self._coupling_np, None, nx)
             self._plan.set_energy_fields(1, kin1, pot, cpl1)
             self._has_ref_energy = True
         else:

@@ -325,9 +325,10 @@ def poisson_arrivals(rate, window, seed):
 
 
 def requests_from_stream(stream, path, device='cuda', dtype=64,
-                         ground_chunk=100, quench_chunk=500):
+                         ground_chunk=100, quench_chunk=500, device_setup=False):
     """``SolveRequest`` objects for ``workloads.served_stream`` descriptions:
-    each builds its PSpinor and drop-in propagator when admitted."""
+    each builds its PSpinor (``device_setup``: a ``DeviceSpinor``, set up on
+    the GPU) and drop-in propagator when admitted."""
     from . import workloads
     from .pspinor import pspinor as spin
     from .pspinor import tensor_propagator as tprop
@@ -336,7 +337,10 @@ def requests_from_stream(stream, path, device='cuda', dtype=64,
 
     def maker(d):
         def make():
-            ps = workloads.request_spin(spin.PSpinor, ttools.fft_2d, path, d)
+            if device_setup:
+                ps = workloads.request_spin_device(path, d, device=device, dtype=bits)
+            else:
+                ps = workloads.request_spin(spin.PSpinor, ttools.fft_2d, path, d)
             return tprop.TensorPropagator(ps, d['dt'], d['max_steps'], device,
                                           time=d['time'], dtype=bits)
         return make

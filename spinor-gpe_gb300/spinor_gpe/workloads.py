@@ -192,3 +192,48 @@ def request_spin(spinor_cls, fft_2d, path, req):
                  half_y=req['half'], g=req['g'], lam=req['lam'],
                  omega=req['omega'], k_l=3.0, delta=req['delta'],
                  rot_coupling=False, seed=req['seed'])
+
+
+def build_device(path, *, nx, ny, half_x, half_y, g, atom_num=1.0, lam=1.0,
+                 omega=None, k_l=None, delta=0.0, rot_coupling=False,
+                 kin_shift=False, seed=0, phase_noise=0.01, vortices=None,
+                 device='cuda', dtype=64):
+    """``build`` with the set-up on the GPU (``DeviceSpinor``): separable
+    operator fields (O(Nx + Ny) host work) and the Thomas-Fermi state,
+    phase noise (a seeded counter hash instead of NumPy's generator) and
+    vortices written by native kernels.  Same problem statement as
+    ``build``; the state differs from it only through the noise draws."""
+    from .pspinor.device_spinor import DeviceSpinor
+    from .pspinor import operators as ops
+    ps = DeviceSpinor(path, overwrite=True, atom_num=atom_num,
+                      mesh_points=(nx, ny), r_sizes=(half_x, half_y),
+                      device=device, dtype=dtype)
+    ps.g_sc = {'uu': float(g[0]), 'dd': float(g[1]), 'ud': float(g[2])}
+    if lam != 1.0:
+        ps.pot_eng = ops.SepField(ps.space['x']**2 / 2, (lam * ps.space['y'])**2 / 2)
+    if omega is not None:
+        ps.coupling_setup(kin_shift=kin_shift)
+        if k_l is not None:
+            ps.kL_recoil = float(k_l)
+        ps.rot_coupling = bool(rot_coupling)
+        ps.coupling_uniform(float(omega))
+        ps.detuning_uniform(float(delta))
+    elif delta:
+        ps.detuning_uniform(float(delta))
+    g_eff = 0.5 * (g[0] + g[2])
+    mu = np.sqrt(g_eff * ps.atom_num * lam / np.pi)
+    amp = np.sqrt(0.5 / g_eff)
+    ps.set_tf_state(mu, [amp, amp], noise=phase_noise, seed=seed, renorm=False)
+    if vortices is not None:
+        positions, windings = vortices
+        ps.seed_vortices(positions, list(windings))
+    return ps
+
+
+def request_spin_device(path, req, device='cuda', dtype=64):
+    """The ``DeviceSpinor`` of one ``served_stream`` request."""
+    return build_device(f"{path}req{req['rid']:06d}/", nx=req['n'], ny=req['n'],
+                        half_x=req['half'], half_y=req['half'], g=req['g'],
+                        lam=req['lam'], omega=req['omega'], k_l=3.0,
+                        delta=req['delta'], rot_coupling=False, seed=req['seed'],
+                        device=device, dtype=dtype)

@@ -105,3 +105,16 @@ def test_oversize_request_rejected():
     req = serve.SolveRequest(0, 0.0, lambda: None, int(2e6), 10)
     with pytest.raises(ValueError):
         srv.run([req])
+
+
+@pytest.mark.gpu
+def test_served_requests_with_device_set_up(tmp_path):
+    stream = workloads.served_stream(rate=200, window=0.02, seed=9,
+                                     ground_sizes=(64,), quench_size=64)
+    for d in stream:
+        d['max_steps'] = 30
+    reqs = serve.requests_from_stream(stream, str(tmp_path) + '/', device_setup=True,
+                                      ground_chunk=10, quench_chunk=10)
+    res = serve.SolveServer(max_active=4).run(reqs, realtime=False)
+    assert len(res) == len(reqs) and all(r.steps > 0 for r in res)
+    assert all(np.isfinite(r.energy) for r in res)

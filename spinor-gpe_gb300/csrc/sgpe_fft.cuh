@@ -26,6 +26,14 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+// Twiddles of a stage whose butterflies sit at j + qT with NS = TQ: one row
+// of table loads and constant roots (1), or a table load per twiddle (0).
+// Off: the product of two rounded factors made the complex64 error after
+// 10^4 steps 35-55% larger for a 1-3% shorter step.
+#ifndef SGPE_TW_FACTOR
+#define SGPE_TW_FACTOR 0
+#endif
+
 #include "sgpe_tc.cuh"
 
 namespace sgpe {
@@ -75,9 +83,28 @@ template <int DIR, int M, class C> __device__ __forceinline__ C tw16(C a) {
   else if constexpr (m == 9) return cmul(a, cmake<C>(-c1, -d * s1));
   else if constexpr (m == 5) return crot<DIR>(cmul(a, cmake<C>(c1, d * s1)));  // W^4 W^1
   else if constexpr (m == 7) return crot<DIR>(cmul(a, cmake<C>(s1, d * c1)));  // W^4 W^3
-  else {
-    static_assert(m == 1 || m == 2 || m == 3 || m == 6 || m == 9, "unused twiddle");
-    return a;
+  else return crot<DIR>(tw16<DIR, m - 4>(a));                                   // 10, 11, 13, 14, 15
+}
+
+// The same with the exponent known only after unrolling (the switch folds).
+template <int DIR, class C> __device__ __forceinline__ C tw16r(C a, int m) {
+  switch (m & 15) {
+    case 0: return a;
+    case 1: return tw16<DIR, 1>(a);
+    case 2: return tw16<DIR, 2>(a);
+    case 3: return tw16<DIR, 3>(a);
+    case 4: return tw16<DIR, 4>(a);
+    case 5: return tw16<DIR, 5>(a);
+    case 6: return tw16<DIR, 6>(a);
+    case 7: return tw16<DIR, 7>(a);
+    case 8: return tw16<DIR, 8>(a);
+    case 9: return tw16<DIR, 9>(a);
+    case 10: return tw16<DIR, 10>(a);
+    case 11: return tw16<DIR, 11>(a);
+    case 12: return tw16<DIR, 12>(a);
+    case 13: return tw16<DIR, 13>(a);
+    case 14: return tw16<DIR, 14>(a);
+    default: return tw16<DIR, 15>(a);
   }
 }
 
@@ -145,6 +172,40 @@ template <int DIR, class C> __device__ __forceinline__ C tw24r(C a, int m) {
     case 21: return tw24<DIR, 21>(a);
     case 22: return tw24<DIR, 22>(a);
     default: return tw24<DIR, 23>(a);
+  }
+}
+
+// a * exp(-2 pi i m / E) for the points-per-thread E of the engine, m known
+// after unrolling.
+template <int E, class C> __device__ __forceinline__ C root_fwd(C a, int m) {
+  if constexpr (E == 16) return tw16r<-1>(a, m);
+  else if constexpr (E == 8) return tw16r<-1>(a, 2 * m);
+  else if constexpr (E == 4) return tw16r<-1>(a, 4 * m);
+  else if constexpr (E == 2) return tw16r<-1>(a, 8 * m);
+  else if constexpr (E == 24) return tw24r<-1>(a, m);
+  else if constexpr (E == 12) return tw24r<-1>(a, 2 * m);
+  else {
+    static_assert(E == 32, "no constant roots for this E");
+    switch (m & 31) {
+      case 0: return a;
+      case 1: return tw32<-1, 1>(a);
+      case 3: return tw32<-1, 3>(a);
+      case 5: return tw32<-1, 5>(a);
+      case 7: return tw32<-1, 7>(a);
+      case 9: return tw32<-1, 9>(a);
+      case 11: return tw32<-1, 11>(a);
+      case 13: return tw32<-1, 13>(a);
+      case 15: return tw32<-1, 15>(a);
+      case 17: return tw32<-1, 17>(a);
+      case 19: return tw32<-1, 19>(a);
+      case 21: return tw32<-1, 21>(a);
+      case 23: return tw32<-1, 23>(a);
+      case 25: return tw32<-1, 25>(a);
+      case 27: return tw32<-1, 27>(a);
+      case 29: return tw32<-1, 29>(a);
+      case 31: return tw32<-1, 31>(a);
+      default: return tw16r<-1>(a, (m & 31) / 2);
+    }
   }
 }
 
@@ -373,7 +434,23 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
         if constexpr (kFirst && !FROM_SMEM) a[l][q][r] = v[l][q + r * Q];
         else a[l][q][r] = sm.ld(l, j + q * T + r * (N / R));
       }
-  if constexpr (!kFirst) {
+  if constexpr (!kFirst && SGPE_TW_FACTOR && Q > 1 && T * Q == NS) {
+    // The Q butterflies of the thread sit at k = j + qT with NS = TQ, so
+    // W_{NS R}^{(j + qT) r} = W_{NS R}^{j r} W_E^{q r}: R - 1 table values
+    // times compile-time roots of order E (instead of Q (R - 1) loads).
+    constexpr int kOff = tw_offset(N, E, NS);
+    C w1[R];
+#pragma unroll
+    for (int r = 1; r < R; ++r) w1[r] = __ldg(tw + kOff + j + (r - 1) * NS);
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        const C w = q == 0 ? w1[r] : root_fwd<E>(w1[r], q * r);
+#pragma unroll
+        for (int l = 0; l < L; ++l) a[l][q][r] = (DIR < 0) ? cmul(a[l][q][r], w) : cmulc(a[l][q][r], w);
+      }
+  } else if constexpr (!kFirst) {
     constexpr int kOff = tw_offset(N, E, NS);
 #pragma unroll
     for (int q = 0; q < Q; ++q) {

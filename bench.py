@@ -69,6 +69,9 @@ def parse():
     ap.add_argument('--serve-rate', type=float, default=200.0)
     ap.add_argument('--serve-window', type=float, default=0.5)
     ap.add_argument('--max-active', type=int, default=64)
+    ap.add_argument('--tensor-core-dft', action='store_true',
+                    help='raman_quench: run the split-BF16 tensor-core DFT16 '
+                         'variant (precision study; not the headline)')
     ap.add_argument('--host-setup', action='store_true',
                     help='served: build each request with the host PSpinor '
                          'set-up instead of the device set-up')
@@ -268,7 +271,8 @@ def run_native(args, world, rank, local):
     psik_host = [torch.as_tensor(np.asarray(p), dtype=torch.complex64)
                  .pin_memory() for p in ps.psik]
     props = [tprop.TensorPropagator(ps, 1e-3, args.steps, device, time='real',
-                                    dtype=64) for _ in range(n_rep)]
+                                    dtype=64, tensor_core_dft=args.tensor_core_dft)
+             for _ in range(n_rep)]
     stream = torch.cuda.current_stream()
 
     # warm-up
@@ -344,7 +348,8 @@ def run_native(args, world, rank, local):
         'steps': k, 'warmup': args.warmup,
         'ms_per_step': 1e3 * t_max / k * 1.0,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
-        'dtype': 'c64 (fp32 butterflies; fp64 reductions)',
+        'dtype': ('c64 (split-BF16 tensor-core DFT16 stages)' if args.tensor_core_dft
+                  else 'c64 (fp32 butterflies; fp64 reductions)'),
         'data': 'synthetic (seeded Thomas-Fermi + phase noise, 3000-step '
                 'imaginary-time preparation)',
         'config': {'workload': f'raman_quench_{n}', 'grid': [n, n],

@@ -200,12 +200,18 @@ template <typename R> struct ColLauncher {
 // 64, 256, 1024, 2048).  Rows: the row configuration with a 128-register
 // cap; columns: 4 columns per block (at least one warp), so the staging
 // tiles of every warp fit in shared memory at 2048.
+#ifndef SGPE_TC_ROW_MINB
+#define SGPE_TC_ROW_MINB 3
+#endif
+#ifndef SGPE_TC_COL_MINB
+#define SGPE_TC_COL_MINB 2
+#endif
 inline bool tc_size_supported(int n) { return n == 64 || n == 256 || n == 1024 || n == 2048; }
 
 template <int N> struct RowTcCfg {
   using B = RowCfg<float, N>;
   static constexpr int E = B::E, ROWS = B::ROWS, THREADS = B::THREADS;
-  static constexpr int MINB = cmax(1, cmin(2, 1024 / THREADS));
+  static constexpr int MINB = cmax(1, cmin(SGPE_TC_ROW_MINB, 1024 / THREADS));
   static constexpr size_t SMEM = ((B::SMEM + 15) & ~size_t(15)) + sizeof(uint32_t) * kTcBfragWords +
                                  size_t(THREADS / 32) * kTcScratchFloats * sizeof(float);
 };
@@ -215,7 +221,7 @@ template <int N> struct ColTcCfg {
   static constexpr int T = N / E;
   static constexpr int COLS = cmax(4, 32 / T);
   static constexpr int THREADS = T * COLS;
-  static constexpr int MINB = 1;
+  static constexpr int MINB = cmax(1, cmin(SGPE_TC_COL_MINB, 1024 / THREADS));
   static constexpr size_t XBYTES = size_t(COLS) * (N + N / E + 2) * sizeof(float2);
   static constexpr size_t SMEM = ((XBYTES + 15) & ~size_t(15)) + sizeof(uint32_t) * kTcBfragWords +
                                  size_t(THREADS / 32) * kTcScratchFloats * sizeof(float);

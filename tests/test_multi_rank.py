@@ -9,7 +9,6 @@ import socket
 import subprocess
 import sys
 
-import pytest
 import torch
 import torch.multiprocessing as mp
 

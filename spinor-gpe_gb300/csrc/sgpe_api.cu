@@ -55,14 +55,22 @@ struct HostField {
 //  coupling  c uniform, s conj(e) and s e x-tables.
 struct SepOps {
   DevField kx[2], ky[2];
-  bool kin = false;
+  bool kin = false, kin_real = false;
   DevField px[2], py[2], s01x, s10x;
   bool pot = false, cpl = false;
 };
 
+// True when every value of the field has a zero imaginary part.
+bool imag_zero(const HostField& f) {
+  for (size_t i = 1; i < f.v.size(); i += 2)
+    if (f.v[i] != 0.0) return false;
+  return true;
+}
+
 struct SubOps {
   DevField kin_a[2], kin_b[2], pot_a[2], pot_b[2], cc, cs, ce, s01, s10;
   bool has_s01 = false;
+  bool pot_real = false, cc_real = false, kin_real = false;
   HostField s01_host, s10_host;  // FP64 off-diagonals when has_s01
   SepOps sep;
   HostField kin_host[2][2];  // [comp][a, b]
@@ -84,6 +92,7 @@ struct EnergyFields {
 struct PairOps {
   DevField a[2], b[2];
   SepOps sep;             // kinetic part only
+  bool real = false;
   std::vector<void*> allocs;
   bool set = false;
 };
@@ -407,6 +416,7 @@ int ensure_pair(sgpe_plan* p, int prev, int next) {
     free_pair(po);
     return rc;
   }
+  po.real = imag_zero(ma[0]) && imag_zero(ma[1]) && imag_zero(mb[0]) && imag_zero(mb[1]);
   po.set = true;
   return SGPE_OK;
 }
@@ -415,19 +425,23 @@ template <typename R> sgpe::Field<R> typed(const DevField& f) {
   return sgpe::Field<R>{static_cast<const sgpe::Cx<R>*>(f.p), f.sx, f.sy};
 }
 
-template <typename R> sgpe::KinOp<R> kin_from(const DevField (&a)[2], const DevField (&b)[2], const SepOps& sep) {
+template <typename R>
+sgpe::KinOp<R> kin_from(const DevField (&a)[2], const DevField (&b)[2], const SepOps& sep, bool real) {
   sgpe::KinOp<R> k;
   for (int c = 0; c < 2; ++c) {
     k.a[c] = typed<R>(sep.kin ? sep.kx[c] : a[c]);
     k.b[c] = typed<R>(sep.kin ? sep.ky[c] : b[c]);
   }
   k.sep = sep.kin ? 1 : 0;
+  k.real = real ? 1 : 0;
   return k;
 }
 
-template <typename R> sgpe::KinOp<R> kin_op(const SubOps& so) { return kin_from<R>(so.kin_a, so.kin_b, so.sep); }
+template <typename R> sgpe::KinOp<R> kin_op(const SubOps& so) {
+  return kin_from<R>(so.kin_a, so.kin_b, so.sep, so.kin_real);
+}
 
-template <typename R> sgpe::KinOp<R> kin_pair(const PairOps& po) { return kin_from<R>(po.a, po.b, po.sep); }
+template <typename R> sgpe::KinOp<R> kin_pair(const PairOps& po) { return kin_from<R>(po.a, po.b, po.sep, po.real); }
 
 template <typename R> sgpe::RealOp<R> real_op(const SubOps& so, int coupling) {
   sgpe::RealOp<R> o;
@@ -443,6 +457,8 @@ template <typename R> sgpe::RealOp<R> real_op(const SubOps& so, int coupling) {
   o.s01 = typed<R>(sep && coupling ? so.sep.s01x : so.has_s01 ? so.s01 : so.cs);
   o.s10 = typed<R>(sep && coupling ? so.sep.s10x : so.has_s01 ? so.s10 : so.cs);
   o.sep = sep ? 1 : 0;
+  o.real_pot = so.pot_real ? 1 : 0;
+  o.real_cc = so.cc_real ? 1 : 0;
   o.zr = R(so.zr);
   o.zi = R(so.zi);
   return o;
@@ -947,6 +963,14 @@ int sgpe_set_substep(sgpe_plan* p, int sub, const sgpe_substep_ops* ops) {
       so.kin_host[c][k].sy = src[k]->sy;
     }
   }
+  // factors with zero imaginary parts (imaginary time)
+  so.kin_real = true;
+  for (int c = 0; c < 2; ++c)
+    for (int k = 0; k < 2; ++k) so.kin_real = so.kin_real && imag_zero(so.kin_host[c][k]);
+  so.pot_real = true;
+  for (int c = 0; c < 2; ++c)
+    so.pot_real = so.pot_real && imag_zero(host_field(ops->pot_a[c])) && imag_zero(host_field(ops->pot_b[c]));
+  so.cc_real = imag_zero(host_field(ops->cpl_c));
   // separable fast-path tables
   {
     const HostField ka[2] = {so.kin_host[0][0], so.kin_host[1][0]};

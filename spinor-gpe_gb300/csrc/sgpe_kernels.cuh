@@ -92,6 +92,7 @@ template <typename R> __device__ __forceinline__ Cx<R> fld(const Field<R>& f, in
 template <typename R> struct KinOp {
   Field<R> a[2], b[2];
   int sep;
+  int real;   // every factor has a zero imaginary part (imaginary time)
 };
 
 // Real-space operators of one sub-step:
@@ -109,6 +110,8 @@ template <typename R> struct RealOp {
   // sep: pa_c, s01, s10 are x-tables of Nx values, pb_c y-tables of Ny
   // values (unit strides), cc is uniform
   int sep;
+  // zero imaginary parts (imaginary time): real multiplies give the same bits
+  int real_pot, real_cc;
   R zr, zi;
 };
 
@@ -393,25 +396,48 @@ __device__ __forceinline__ void apply_real_ops(Cx<R>& p0, Cx<R>& p1, const Point
   const R e1 = fmadd(a.g_dd, n1, a.g_ud * n0);
   const C i0 = cexp_z(op.zr, op.zi, e0);
   const C i1 = cexp_z(op.zr, op.zi, e1);
-  p0 = cmul(p0, i0);
-  p1 = cmul(p1, i1);
+  // Factors with zero imaginary parts are applied as real scalings: for
+  // b = (x, 0), cmul(a, b) = (fma(a.x, x, -0), fma(a.x, 0, a.y x)) is
+  // bit-identical to (a.x x, a.y x).
+  const bool ireal = (op.zi == R(0));
+  if (ireal) {
+    p0 = cscale(p0, i0.x);
+    p1 = cscale(p1, i1.x);
+  } else {
+    p0 = cmul(p0, i0);
+    p1 = cmul(p1, i1);
+  }
   const C cc = v.cc, s01 = v.s01, s10 = v.s10;
   if (a.coupling) {
-    const C q0 = cadd(cmul(cc, p0), cmul(s01, p1));
-    const C q1 = cadd(cmul(s10, p0), cmul(cc, p1));
+    const C c0 = op.real_cc ? cscale(p0, cc.x) : cmul(cc, p0);
+    const C c1 = op.real_cc ? cscale(p1, cc.x) : cmul(cc, p1);
+    const C q0 = cadd(c0, cmul(s01, p1));
+    const C q1 = cadd(cmul(s10, p0), c1);
     p0 = q0;
     p1 = q1;
   }
-  p0 = cmul(p0, cmul(v.pa0, v.pb0));
-  p1 = cmul(p1, cmul(v.pa1, v.pb1));
+  if (op.real_pot) {
+    p0 = cscale(p0, v.pa0.x * v.pb0.x);
+    p1 = cscale(p1, v.pa1.x * v.pb1.x);
+  } else {
+    p0 = cmul(p0, cmul(v.pa0, v.pb0));
+    p1 = cmul(p1, cmul(v.pa1, v.pb1));
+  }
   if (a.coupling) {
-    const C q0 = cadd(cmul(cc, p0), cmul(s01, p1));
-    const C q1 = cadd(cmul(s10, p0), cmul(cc, p1));
+    const C c0 = op.real_cc ? cscale(p0, cc.x) : cmul(cc, p0);
+    const C c1 = op.real_cc ? cscale(p1, cc.x) : cmul(cc, p1);
+    const C q0 = cadd(c0, cmul(s01, p1));
+    const C q1 = cadd(cmul(s10, p0), c1);
     p0 = q0;
     p1 = q1;
   }
-  p0 = cmul(p0, i0);
-  p1 = cmul(p1, i1);
+  if (ireal) {
+    p0 = cscale(p0, i0.x);
+    p1 = cscale(p1, i1.x);
+  } else {
+    p0 = cmul(p0, i0);
+    p1 = cmul(p1, i1);
+  }
 }
 
 // The same with the operator values read through the generic broadcast
@@ -449,8 +475,13 @@ __device__ __forceinline__ void apply_kinetic(Cx<R> (&v)[E], const KinOp<R>& k, 
   if (k.sep) {  // x-table times y-table, unit strides
     const C ka = __ldg(k.a[comp].p + x);
     const C* kb = k.b[comp].p + j;
+    if (k.real) {  // same bits as the complex products (see apply_real_ops)
 #pragma unroll
-    for (int m = 0; m < E; ++m) v[m] = cmul(v[m], cmul(ka, __ldg(kb + m * T)));
+      for (int m = 0; m < E; ++m) v[m] = cscale(v[m], ka.x * __ldg(&kb[m * T].x));
+    } else {
+#pragma unroll
+      for (int m = 0; m < E; ++m) v[m] = cmul(v[m], cmul(ka, __ldg(kb + m * T)));
+    }
     return;
   }
   const Field<R>& fa = k.a[comp];

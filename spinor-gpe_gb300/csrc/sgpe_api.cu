@@ -198,13 +198,23 @@ struct sgpe_batch {
 
 namespace {
 
+// One twiddle-table entry from an FP64 value: rounded once, or as FP32 head
+// and tail (SGPE_TW_COMP).
+template <class W> W twiddle_entry(double re, double im);
+template <> inline float2 twiddle_entry<float2>(double re, double im) { return make_float2(float(re), float(im)); }
+template <> inline double2 twiddle_entry<double2>(double re, double im) { return make_double2(re, im); }
+template <> inline float4 twiddle_entry<float4>(double re, double im) {
+  const float hr = float(re), hi = float(im);
+  return make_float4(hr, hi, float(re - double(hr)), float(im - double(hi)));
+}
+
 // Per-stage twiddle table of an (n, e) transform, in the order the FFT
 // engine reads it (sgpe_fft.cuh: tw_offset): for each stage (ns, r_s),
 // entries exp(-2 pi i k r / (ns r_s)) at (r - 1) * ns + k.  Angles are
 // reduced exactly in integers and evaluated in FP64, then rounded once.
 template <typename R> void* upload_twiddles(int n, int e, cudaError_t* err) {
-  using C = sgpe::Cx<R>;
-  std::vector<C> h;
+  using W = sgpe::TwE<R>;
+  std::vector<W> h;
   const double two_pi = 6.283185307179586476925286766559;
   for (int ns = 1; ns < n;) {
     const int rs = sgpe::stage_radix(n, e, ns);
@@ -213,18 +223,15 @@ template <typename R> void* upload_twiddles(int n, int e, cudaError_t* err) {
       for (int k = 0; k < ns; ++k) {
         const long long m = ((long long)k * r) % len;
         const double ang = two_pi * double(m) / double(len);
-        C c;
-        c.x = R(std::cos(ang));
-        c.y = R(-std::sin(ang));
-        h.push_back(c);
+        h.push_back(twiddle_entry<W>(std::cos(ang), -std::sin(ang)));
       }
     ns *= rs;
   }
-  if (h.empty()) h.push_back(C{R(1), R(0)});
+  if (h.empty()) h.push_back(twiddle_entry<W>(1.0, 0.0));
   void* d = nullptr;
-  *err = cudaMalloc(&d, sizeof(C) * h.size());
+  *err = cudaMalloc(&d, sizeof(W) * h.size());
   if (*err != cudaSuccess) return nullptr;
-  *err = cudaMemcpy(d, h.data(), sizeof(C) * h.size(), cudaMemcpyHostToDevice);
+  *err = cudaMemcpy(d, h.data(), sizeof(W) * h.size(), cudaMemcpyHostToDevice);
   return d;
 }
 

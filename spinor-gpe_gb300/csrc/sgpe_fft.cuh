@@ -26,6 +26,14 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+// Complex64 twiddles stored as head + tail (float4: hi.x, hi.y, lo.x, lo.y,
+// lo = the FP32 rounding of the FP64 remainder), applied as a*hi + a*lo: the
+// table values then carry ~48 bits instead of 24, which removes the
+// systematic (same every step) error of rounded twiddles.  (1) on, (0) off.
+#ifndef SGPE_TW_COMP
+#define SGPE_TW_COMP 0
+#endif
+
 // Twiddles of a stage whose butterflies sit at j + qT with NS = TQ: one row
 // of table loads and constant roots (1), or a table load per twiddle (0).
 // Off: the product of two rounded factors made the complex64 error after
@@ -43,6 +51,13 @@ template <> struct CxT<float> { using type = float2; };
 template <> struct CxT<double> { using type = double2; };
 template <typename R> using Cx = typename CxT<R>::type;
 
+// Element type of the twiddle tables (see SGPE_TW_COMP).
+template <typename R> struct TwT { using type = Cx<R>; };
+#if SGPE_TW_COMP
+template <> struct TwT<float> { using type = float4; };
+#endif
+template <typename R> using TwE = typename TwT<R>::type;
+
 __device__ __forceinline__ float fmadd(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double fmadd(double a, double b, double c) { return __fma_rn(a, b, c); }
 
@@ -59,6 +74,20 @@ template <class C> __device__ __forceinline__ C cmulc(C a, C b) {
   return cmake<C>(fmadd(a.x, b.x, a.y * b.y), fmadd(a.y, b.x, -a.x * b.y));
 }
 template <class C> __device__ __forceinline__ C cscale(C a, decltype(C::x) s) { return cmake<C>(a.x * s, a.y * s); }
+
+// a * w (DIR < 0) or a * conj(w) (DIR > 0) for a twiddle-table entry: a
+// complex value, or a head + tail pair (float4) multiplied as a*hi + a*lo.
+template <int DIR, class C> __device__ __forceinline__ C tw_mul(C a, C w) {
+  return DIR < 0 ? cmul(a, w) : cmulc(a, w);
+}
+template <int DIR> __device__ __forceinline__ float2 tw_mul(float2 a, float4 w) {
+  if (DIR < 0) {
+    const float tr = fmadd(a.x, w.z, -a.y * w.w), ti = fmadd(a.x, w.w, a.y * w.z);
+    return make_float2(fmadd(a.x, w.x, fmadd(-a.y, w.y, tr)), fmadd(a.x, w.y, fmadd(a.y, w.x, ti)));
+  }
+  const float tr = fmadd(a.x, w.z, a.y * w.w), ti = fmadd(a.y, w.z, -a.x * w.w);
+  return make_float2(fmadd(a.x, w.x, fmadd(a.y, w.y, tr)), fmadd(a.y, w.x, fmadd(-a.x, w.y, ti)));
+}
 template <class C> __device__ __forceinline__ decltype(C::x) cabs2(C a) { return fmadd(a.x, a.x, a.y * a.y); }
 // a * (DIR * i): DIR = -1 gives a * (-i), DIR = +1 gives a * i
 template <int DIR, class C> __device__ __forceinline__ C crot(C a) {
@@ -439,6 +468,7 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
     // W_{NS R}^{(j + qT) r} = W_{NS R}^{j r} W_E^{q r}: R - 1 table values
     // times compile-time roots of order E (instead of Q (R - 1) loads).
     constexpr int kOff = tw_offset(N, E, NS);
+    static_assert(sizeof(TwE<decltype(C::x)>) == sizeof(C), "factorised twiddles need plain tables");
     C w1[R];
 #pragma unroll
     for (int r = 1; r < R; ++r) w1[r] = __ldg(tw + kOff + j + (r - 1) * NS);
@@ -455,12 +485,13 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       const int vt = j + q * T;
-      const C* twq = tw + kOff + (vt % NS);
+      using W = TwE<decltype(C::x)>;
+      const W* twq = reinterpret_cast<const W*>(tw) + kOff + (vt % NS);
 #pragma unroll
       for (int r = 1; r < R; ++r) {
-        const C w = __ldg(twq + (r - 1) * NS);
+        const W w = __ldg(twq + (r - 1) * NS);
 #pragma unroll
-        for (int l = 0; l < L; ++l) a[l][q][r] = (DIR < 0) ? cmul(a[l][q][r], w) : cmulc(a[l][q][r], w);
+        for (int l = 0; l < L; ++l) a[l][q][r] = tw_mul<DIR>(a[l][q][r], w);
       }
     }
   }

@@ -62,8 +62,15 @@ int scratch_address(void** out) {
 // Per-stage twiddle table of an (n, e) transform in the order the FFT engine
 // reads it (sgpe_fft.cuh): stage (ns, r_s) holds exp(-2 pi i k r/(ns r_s)) at
 // (r - 1) ns + k.  FP64 sincospi of the exactly reduced fraction, rounded once.
+__device__ __forceinline__ void set_twiddle(float2& w, double re, double im) { w = make_float2(float(re), float(im)); }
+__device__ __forceinline__ void set_twiddle(double2& w, double re, double im) { w = make_double2(re, im); }
+__device__ __forceinline__ void set_twiddle(float4& w, double re, double im) {
+  const float hr = float(re), hi = float(im);
+  w = make_float4(hr, hi, float(re - double(hr)), float(im - double(hi)));
+}
+
 template <typename R>
-__global__ void twiddle_kernel(sgpe::Cx<R>* out, int n, int e, int total) {
+__global__ void twiddle_kernel(sgpe::TwE<R>* out, int n, int e, int total) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= total) return;
   int off = 0, ns = 1;
@@ -76,8 +83,7 @@ __global__ void twiddle_kernel(sgpe::Cx<R>* out, int n, int e, int total) {
       const long long m = ((long long)k * r) % len;
       double sn, cs;
       sincospi(2.0 * double(m) / double(len), &sn, &cs);
-      out[i].x = R(cs);
-      out[i].y = R(-sn);
+      set_twiddle(out[i], cs, -sn);
       return;
     }
     off += cnt;
@@ -96,8 +102,9 @@ int run(int ny, int nx, const void* i0, const void* i1, void* o0, void* o1, int 
   if (ex == 0 || ey == 0 || cols == 0 || nx % cols != 0 || (nx / 2) % cols != 0)
     return sgpe_detail::set_error(SGPE_ERR_ARG, "fft2_static: unsupported grid size");
   const int twx = sgpe::tw_offset(nx, ex, nx), twy = sgpe::tw_offset(ny, ey, ny);
+  using W = sgpe::TwE<R>;
   const size_t field = round_up(sizeof(C) * (size_t)nx * ny);
-  const size_t need = 2 * field + round_up(sizeof(C) * (twx > 0 ? twx : 1)) + round_up(sizeof(C) * (twy > 0 ? twy : 1));
+  const size_t need = 2 * field + round_up(sizeof(W) * (twx > 0 ? twx : 1)) + round_up(sizeof(W) * (twy > 0 ? twy : 1));
   if (need > size_t(SGPE_FFT2_STATIC_BYTES))
     return sgpe_detail::set_error(
         SGPE_ERR_ARG, "fft2_static: a " + std::to_string(ny) + "x" + std::to_string(nx) + " complex" +
@@ -110,17 +117,17 @@ int run(int ny, int nx, const void* i0, const void* i1, void* o0, void* o1, int 
   unsigned char* b = static_cast<unsigned char*>(base);
   C* mid0 = reinterpret_cast<C*>(b);
   C* mid1 = reinterpret_cast<C*>(b + field);
-  C* tw_x = reinterpret_cast<C*>(b + 2 * field);
-  C* tw_y = reinterpret_cast<C*>(b + 2 * field + round_up(sizeof(C) * (twx > 0 ? twx : 1)));
+  W* tw_x = reinterpret_cast<W*>(b + 2 * field);
+  W* tw_y = reinterpret_cast<W*>(b + 2 * field + round_up(sizeof(W) * (twx > 0 ? twx : 1)));
   if (twx > 0) twiddle_kernel<R><<<(twx + 255) / 256, 256, 0, s>>>(tw_x, nx, ex, twx);
   if (twy > 0) twiddle_kernel<R><<<(twy + 255) / 256, 256, 0, s>>>(tw_y, ny, ey, twy);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return sgpe_detail::set_error(SGPE_ERR_CUDA, std::string("fft2_static: ") + cudaGetErrorString(e));
 
   sgpe::RowArgs<R> r{};
-  r.tw = tw_x;
+  r.tw = reinterpret_cast<const C*>(tw_x);
   sgpe::ColArgs<R> c{};
-  c.tw = tw_y;
+  c.tw = reinterpret_cast<const C*>(tw_y);
   c.nx = nx;
   c.scale = R(1);
   if (!inverse) {  // x transform into the scratch, then y transform with centring

@@ -241,6 +241,34 @@ int sgpe_batch_steps(sgpe_batch* batch, int n_steps, void* stream);
  * No counterpart in the original. */
 int sgpe_set_dft_mode(sgpe_plan* plan, int mode);
 
+/* Kernel shapes.  Each pass (axis 0: the row pass along x, axis 1: the
+ * column pass along y) can run in one of several launch configurations for
+ * the same side: shape 0 and, for power-of-two sides up to 512, shapes with
+ * fewer points per thread (more threads per line, more transform stages),
+ * which give small grids more warps per SM.  All shapes compute the same
+ * steps; rounding differs with the radix plan (every shape meets the parity
+ * tolerances).  A new plan takes built-in defaults measured on GB300.
+ * No counterpart in the original (whose transforms are cuFFT's).
+ *
+ * sgpe_shape_count: number of shapes for (dtype_bits, axis, side n), 0 if n
+ * is unsupported.  sgpe_set_shapes: switch the plan's shapes (new twiddle
+ * tables, graphs re-captured; the state is kept; the tensor-core DFT mode
+ * runs shape 0 only).  sgpe_get_shapes: the current shapes. */
+#define SGPE_MAX_SHAPES 3
+int sgpe_shape_count(int dtype_bits, int axis, int n);
+int sgpe_set_shapes(sgpe_plan* plan, int row_shape, int col_shape);
+int sgpe_get_shapes(const sgpe_plan* plan, int* row_shape, int* col_shape);
+
+/* Autotuner: times n_steps steady-state full steps in every pair of
+ * shapes (twice, the faster kept), each pair starting from the plan's
+ * current state, and leaves the plan in the fastest pair with that state
+ * restored (the plan's own shapes stay unless another pair is more than 2%
+ * faster).  step_us (optional, SGPE_MAX_SHAPES^2 entries, index
+ * row_shape * SGPE_MAX_SHAPES + col_shape) receives the microseconds per
+ * step, -1 for pairs not run.  Synchronises `stream`.  The plan must be
+ * ready to step, with no populations pending. */
+int sgpe_autotune(sgpe_plan* plan, int n_steps, int* row_shape, int* col_shape, double* step_us, void* stream);
+
 /* Size in bytes of the device scratch array used by sgpe_fft2_static
  * (2.25 MiB, present on every GPU that loads the library). */
 #define SGPE_FFT2_STATIC_BYTES (2359296)

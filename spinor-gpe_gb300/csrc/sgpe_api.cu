@@ -135,6 +135,8 @@ struct sgpe_plan {
   int ntile = 0;             // column tiles of the current kernels
   int ntile_fp32 = 0;        // ... of the FP32 DFT kernels
   int tc = 0;                // radix-16 stages on the tensor cores (split-BF16)
+  int row_shape = 0;         // kernel shapes of the row (x) and column (y)
+  int col_shape = 0;         // passes (sgpe_launch.cuh); twiddles follow them
   uint32_t* tcb = nullptr;   // their B fragments (device)
   void* tw_x = nullptr;
   void* tw_y = nullptr;
@@ -176,6 +178,7 @@ constexpr int kGraphSteps = 8;
 struct BatchGroup {
   std::vector<int> members;  // indices into sgpe_batch::plans
   int nx = 0, ny = 0, bits = 0;
+  int row_shape = 0, col_shape = 0;  // the members' kernel shapes (equal)
   void* col_args = nullptr;  // device ColArgs[3][G]: (0 -> 0), (0 -> 1), (1 -> 0)
   void* row_args = nullptr;  // device RowArgs[2][G]: sub-steps 0, 1
   cudaStream_t stream = nullptr;
@@ -233,6 +236,32 @@ template <typename R> void* upload_twiddles(int n, int e, cudaError_t* err) {
   if (*err != cudaSuccess) return nullptr;
   *err = cudaMemcpy(d, h.data(), sizeof(W) * h.size(), cudaMemcpyHostToDevice);
   return d;
+}
+
+// Default kernel shape of a pass (axis 0: rows along x, 1: columns along y)
+// for a side n, from single-solve step times of square grids measured on
+// GB300 with sgpe_autotune (real and imaginary time ranked alike): fewer
+// points per thread win where a grid is too small to give every SM enough
+// warps, and for complex128 wherever the FP64 butterflies of few blocks set
+// the pace.  Step times (us), shape (0,0) -> default:
+//   complex64   32^2 24 -> 15, 64^2 26 -> 15, 128^2 27 -> 16,
+//              256^2 29 -> 21, 512^2 69 -> 40;
+//   complex128  64^2 234 -> 131, 128^2 258 -> 145, 256^2 325 -> 182.
+int default_shape(int bits, int axis, int n) {
+  struct Entry {
+    int n, row, col;
+  };
+  static const Entry f32[] = {{32, 2, 1}, {64, 2, 2}, {128, 2, 1}, {256, 2, 0}, {512, 1, 0}};
+  static const Entry f64[] = {{32, 1, 1}, {64, 1, 1}, {128, 1, 1}, {256, 1, 1}, {512, 0, 0}};
+  for (const Entry& x : (bits == 64 ? f32 : f64))
+    if (x.n == n) return axis == 0 ? x.row : x.col;
+  return 0;
+}
+
+int shape_count(int bits, int axis, int n) {
+  if (!sgpe::size_supported(n)) return 0;
+  if (bits == 64) return axis == 0 ? sgpe::row_shape_count<float>(n) : sgpe::col_shape_count<float>(n);
+  return axis == 0 ? sgpe::row_shape_count<double>(n) : sgpe::col_shape_count<double>(n);
 }
 
 void free_sub(SubOps& so) {
@@ -490,6 +519,7 @@ template <typename R> bool col_step_args(sgpe_plan* p, int sub, bool want_u, sgp
   a.tw = cst<R>(p->tw_y);
   a.tc = p->tc;
   a.tcb = p->tcb;
+  a.shape = p->col_shape;
   a.nx = p->nx;
   a.fwd = (p->form == kMixed);
   a.inv = 1;
@@ -526,6 +556,7 @@ template <typename R> sgpe::RowArgs<R> row_step_args(sgpe_plan* p, int sub, doub
   a.tw = cst<R>(p->tw_x);
   a.tc = p->tc;
   a.tcb = p->tcb;
+  a.shape = p->row_shape;
   a.mode = sgpe::kRowStep;
   a.scale = R(1);
   a.part = reinterpret_cast<R*>(p->part);
@@ -581,6 +612,7 @@ template <typename R> int store(sgpe_plan* p, void* o0, void* o1, double* pops, 
   a.tw = cst<R>(p->tw_y);
   a.tc = p->tc;
   a.tcb = p->tcb;
+  a.shape = p->col_shape;
   a.nx = p->nx;
   a.fwd = 1;
   a.inv = 0;
@@ -617,10 +649,12 @@ template <typename R> int fft2(sgpe_plan* p, const void* i0, const void* i1, voi
   r.tw = cst<R>(p->tw_x);
   r.tc = p->tc;
   r.tcb = p->tcb;
+  r.shape = p->row_shape;
   sgpe::ColArgs<R> c{};
   c.tw = cst<R>(p->tw_y);
   c.tc = p->tc;
   c.tcb = p->tcb;
+  c.shape = p->col_shape;
   c.nx = p->nx;
   c.scale = R(1);
   cudaError_t e;
@@ -762,6 +796,51 @@ template <typename R> int capture_steps(sgpe_plan* p, int steps, cudaGraphExec_t
   return SGPE_OK;
 }
 
+// Switch the plan's kernel shapes: new twiddle tables for an axis whose
+// shape changes, the column-tile count, and the captured graphs dropped.
+// The mixed state is the same in every shape, so this is valid between any
+// two calls.
+template <typename R> int apply_shapes(sgpe_plan* p, int rs, int cs) {
+  if (rs < 0 || rs >= shape_count(p->bits, 0, p->nx) || cs < 0 || cs >= shape_count(p->bits, 1, p->ny))
+    return fail(SGPE_ERR_ARG, "kernel shape out of range for this grid (sgpe_shape_count)");
+  if (p->tc && (rs != 0 || cs != 0)) return fail(SGPE_ERR_STATE, "the tensor-core DFT mode runs shape 0 only");
+  if (rs == p->row_shape && cs == p->col_shape) return SGPE_OK;
+  const int cols = sgpe::col_tile_width<R>(p->ny, cs);
+  if (cols == 0 || p->nx % cols != 0 || (p->nx / 2) % cols != 0)
+    return fail(SGPE_ERR_ARG, "nx incompatible with the column tile width of that shape");
+  DeviceGuard g(p->device);
+  cudaError_t e = cudaSuccess;
+  void* tx = nullptr;
+  void* ty = nullptr;
+  if (rs != p->row_shape) tx = upload_twiddles<R>(p->nx, sgpe::row_points_per_thread<R>(p->nx, rs), &e);
+  if (e == cudaSuccess && cs != p->col_shape)
+    ty = upload_twiddles<R>(p->ny, sgpe::col_points_per_thread<R>(p->ny, cs), &e);
+  if (e != cudaSuccess) {
+    if (tx) cudaFree(tx);
+    if (ty) cudaFree(ty);
+    return fail(SGPE_ERR_OOM, std::string("twiddle tables: ") + cudaGetErrorString(e));
+  }
+  drop_graphs(p);
+  // cudaFree waits for launches still reading the old tables
+  if (tx) {
+    cudaFree(p->tw_x);
+    p->tw_x = tx;
+  }
+  if (ty) {
+    cudaFree(p->tw_y);
+    p->tw_y = ty;
+  }
+  p->row_shape = rs;
+  p->col_shape = cs;
+  p->ntile_fp32 = p->nx / cols;
+  p->ntile = p->ntile_fp32;
+  return SGPE_OK;
+}
+
+int apply_shapes_any(sgpe_plan* p, int rs, int cs) {
+  return p->bits == 64 ? apply_shapes<float>(p, rs, cs) : apply_shapes<double>(p, rs, cs);
+}
+
 template <typename R> int full_steps_impl(sgpe_plan* p, int n_steps, double* pops, cudaStream_t s) {
   int i = 0;
   while (i < n_steps) {
@@ -812,7 +891,15 @@ int sgpe_plan_create(sgpe_plan** out, int ny, int nx, int dtype_bits, int device
   // SGPE_DISABLE_GRAPHS (any value) makes this plan launch every step
   // eagerly; used to check graph replay against eager launches.
   p->graphs_enabled = std::getenv("SGPE_DISABLE_GRAPHS") == nullptr;
-  const int cols = dtype_bits == 64 ? sgpe::col_tile_width<float>(ny) : sgpe::col_tile_width<double>(ny);
+  p->row_shape = default_shape(dtype_bits, 0, nx);
+  p->col_shape = default_shape(dtype_bits, 1, ny);
+  int cols = dtype_bits == 64 ? sgpe::col_tile_width<float>(ny, p->col_shape)
+                              : sgpe::col_tile_width<double>(ny, p->col_shape);
+  if (cols == 0 || nx % cols != 0 || (nx / 2) % cols != 0) {
+    // the default shape's tile does not divide nx: shape 0
+    p->col_shape = 0;
+    cols = dtype_bits == 64 ? sgpe::col_tile_width<float>(ny) : sgpe::col_tile_width<double>(ny);
+  }
   if (cols == 0 || nx % cols != 0 || (nx / 2) % cols != 0) {
     delete p;
     return fail(SGPE_ERR_ARG, "nx incompatible with the column tile width");
@@ -827,11 +914,13 @@ int sgpe_plan_create(sgpe_plan** out, int ny, int nx, int dtype_bits, int device
   if (e == cudaSuccess) e = cudaMemset(p->part, 0, red_bytes);
   if (e == cudaSuccess) {
     if (dtype_bits == 64) {
-      p->tw_x = upload_twiddles<float>(nx, sgpe::row_points_per_thread<float>(nx), &e);
-      if (e == cudaSuccess) p->tw_y = upload_twiddles<float>(ny, sgpe::col_points_per_thread<float>(ny), &e);
+      p->tw_x = upload_twiddles<float>(nx, sgpe::row_points_per_thread<float>(nx, p->row_shape), &e);
+      if (e == cudaSuccess)
+        p->tw_y = upload_twiddles<float>(ny, sgpe::col_points_per_thread<float>(ny, p->col_shape), &e);
     } else {
-      p->tw_x = upload_twiddles<double>(nx, sgpe::row_points_per_thread<double>(nx), &e);
-      if (e == cudaSuccess) p->tw_y = upload_twiddles<double>(ny, sgpe::col_points_per_thread<double>(ny), &e);
+      p->tw_x = upload_twiddles<double>(nx, sgpe::row_points_per_thread<double>(nx, p->row_shape), &e);
+      if (e == cudaSuccess)
+        p->tw_y = upload_twiddles<double>(ny, sgpe::col_points_per_thread<double>(ny, p->col_shape), &e);
     }
   }
   if (e != cudaSuccess) {
@@ -889,6 +978,11 @@ int sgpe_set_dft_mode(sgpe_plan* p, int mode) {
   }
   if (p->form == kMixed && p->pending_pops != nullptr)
     return fail(SGPE_ERR_STATE, "populations of the last step are pending; read the state first");
+  if (mode == 1) {
+    // the tensor-core kernels are built on shape 0 (radix-16 stages)
+    const int rc = apply_shapes_any(p, 0, 0);
+    if (rc != SGPE_OK) return rc;
+  }
   if (mode == 1 && p->tcb == nullptr) {
     DeviceGuard g(p->device);
     cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p->tcb), sizeof(uint32_t) * sgpe::kTcBfragWords);
@@ -1232,6 +1326,132 @@ int sgpe_time_passes(sgpe_plan* p, int n_steps, double* col_ms, double* row_ms, 
   return SGPE_OK;
 }
 
+int sgpe_shape_count(int dtype_bits, int axis, int n) {
+  if ((dtype_bits != 64 && dtype_bits != 128) || (axis != 0 && axis != 1)) return 0;
+  return shape_count(dtype_bits, axis, n);
+}
+
+int sgpe_set_shapes(sgpe_plan* p, int row_shape, int col_shape) {
+  if (p == nullptr) return fail(SGPE_ERR_ARG, "null plan");
+  if (p->form == kMixed && p->pending_pops != nullptr)
+    return fail(SGPE_ERR_STATE, "populations of the last step are pending; read the state first");
+  return apply_shapes_any(p, row_shape, col_shape);
+}
+
+int sgpe_get_shapes(const sgpe_plan* p, int* row_shape, int* col_shape) {
+  if (p == nullptr || row_shape == nullptr || col_shape == nullptr) return fail(SGPE_ERR_ARG, "null argument");
+  *row_shape = p->row_shape;
+  *col_shape = p->col_shape;
+  return SGPE_OK;
+}
+
+int sgpe_autotune(sgpe_plan* p, int n_steps, int* row_shape, int* col_shape, double* step_us, void* stream) {
+  if (p == nullptr || row_shape == nullptr || col_shape == nullptr || n_steps < 1)
+    return fail(SGPE_ERR_ARG, "null plan/outputs or n_steps < 1");
+  if (p->form == kEmpty) return fail(SGPE_ERR_STATE, "no state loaded");
+  if (!ready(p)) return fail(SGPE_ERR_STATE, "physics or sub-step operators not set");
+  if (p->form == kMixed && p->pending_pops != nullptr)
+    return fail(SGPE_ERR_STATE, "populations of the last step are pending; read the state first");
+  DeviceGuard g(p->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  constexpr int M = sgpe::kMaxShapes;
+  if (step_us != nullptr)
+    for (int i = 0; i < M * M; ++i) step_us[i] = -1.0;
+  const int nr = shape_count(p->bits, 0, p->nx), nc = shape_count(p->bits, 1, p->ny);
+  const int r0 = p->row_shape, c0 = p->col_shape;
+  *row_shape = r0;
+  *col_shape = c0;
+  if (p->tc || (nr <= 1 && nc <= 1)) return SGPE_OK;
+  // the state is saved and every candidate starts from it; the plan ends
+  // with the saved state in the chosen shapes
+  const size_t bytes = p->elem * (size_t)p->nx * p->ny;
+  for (int c = 0; c < 2; ++c) {
+    if (p->scratch[c] == nullptr) {
+      cudaError_t e = cudaMalloc(&p->scratch[c], bytes);
+      if (e != cudaSuccess) return fail(SGPE_ERR_OOM, std::string("autotune scratch: ") + cudaGetErrorString(e));
+    }
+  }
+  const int form0 = p->form, prev0 = p->prev_sub;
+  auto restore = [&](void* const* from, void* const* to) {
+    cudaError_t e = cudaSuccess;
+    for (int c = 0; c < 2 && e == cudaSuccess; ++c) e = cudaMemcpyAsync(to[c], from[c], bytes, cudaMemcpyDeviceToDevice, s);
+    return e;
+  };
+  cudaError_t e = restore(p->s, p->scratch);
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  for (auto& x : ev)
+    if (e == cudaSuccess) e = cudaEventCreate(&x);
+  std::vector<double> t(M * M, -1.0);
+  int rc = e == cudaSuccess ? SGPE_OK : cuda_fail(e, "autotune set-up");
+  for (int round = 0; round < 2 && rc == SGPE_OK; ++round)
+    for (int r = 0; r < nr && rc == SGPE_OK; ++r)
+      for (int c = 0; c < nc && rc == SGPE_OK; ++c) {
+        if (apply_shapes_any(p, r, c) != SGPE_OK) continue;  // tile width does not divide nx
+        e = restore(p->scratch, p->s);
+        if (e != cudaSuccess) {
+          rc = cuda_fail(e, "autotune restore");
+          break;
+        }
+        p->form = form0;
+        p->prev_sub = prev0;
+        p->pending_pops = nullptr;
+        // warm-up: reaches the steady state and captures both step graphs
+        rc = p->bits == 64 ? full_steps_impl<float>(p, kGraphSteps + 2, nullptr, s)
+                           : full_steps_impl<double>(p, kGraphSteps + 2, nullptr, s);
+        if (rc != SGPE_OK) break;
+        e = cudaEventRecord(ev[0], s);
+        if (e == cudaSuccess) {
+          rc = p->bits == 64 ? full_steps_impl<float>(p, n_steps, nullptr, s)
+                             : full_steps_impl<double>(p, n_steps, nullptr, s);
+          if (rc != SGPE_OK) break;
+          e = cudaEventRecord(ev[1], s);
+        }
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+        if (e != cudaSuccess) {
+          rc = cuda_fail(e, "autotune timing");
+          break;
+        }
+        const double us = 1e3 * ms / n_steps;
+        double& slot = t[r * M + c];
+        slot = (slot < 0 || us < slot) ? us : slot;
+      }
+  for (auto& x : ev)
+    if (x) cudaEventDestroy(x);
+  // fastest shapes; the plan's own stay unless another is >2% faster
+  int br = r0, bc = c0;
+  double bt = t[r0 * M + c0];
+  for (int i = 0; i < M * M; ++i)
+    if (t[i] > 0 && (bt < 0 || t[i] < bt)) {
+      bt = t[i];
+      br = i / M;
+      bc = i % M;
+    }
+  if (t[r0 * M + c0] > 0 && t[r0 * M + c0] <= 1.02 * bt) {
+    br = r0;
+    bc = c0;
+  }
+  if (rc != SGPE_OK) {
+    br = r0;
+    bc = c0;
+  }
+  const int rc2 = apply_shapes_any(p, br, bc);
+  e = restore(p->scratch, p->s);
+  p->form = form0;
+  p->prev_sub = prev0;
+  p->pending_pops = nullptr;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (rc != SGPE_OK) return rc;
+  if (rc2 != SGPE_OK) return rc2;
+  if (e != cudaSuccess) return cuda_fail(e, "autotune restore");
+  *row_shape = br;
+  *col_shape = bc;
+  if (step_us != nullptr)
+    for (int i = 0; i < M * M; ++i) step_us[i] = t[i];
+  return SGPE_OK;
+}
+
 int sgpe_batch_create(sgpe_batch** out, sgpe_plan* const* plans, int n_plans) {
   if (out == nullptr || plans == nullptr || n_plans < 1) return fail(SGPE_ERR_ARG, "null output/plans or no plans");
   *out = nullptr;
@@ -1330,15 +1550,16 @@ template <typename R> int launch_group_steps(const BatchGroup& g, int steps) {
   const int cv[3] = {0, 1, 2}, rs[3] = {0, 1, 0};
   for (int k = 0; k < steps; ++k)
     for (int t = 0; t < 3; ++t) {
-      cudaError_t e = sgpe::launch_col_grouped<R>(col + cv[t] * G, G, g.nx, g.ny, g.stream);
-      if (e == cudaSuccess) e = sgpe::launch_row_grouped<R>(row + rs[t] * G, G, g.nx, g.ny, g.stream);
+      cudaError_t e = sgpe::launch_col_grouped<R>(col + cv[t] * G, g.col_shape, G, g.nx, g.ny, g.stream);
+      if (e == cudaSuccess)
+        e = sgpe::launch_row_grouped<R>(row + rs[t] * G, g.row_shape, G, g.nx, g.ny, g.stream);
       if (e != cudaSuccess) return cuda_fail(e, "batch grouped pass");
     }
   return SGPE_OK;
 }
 
-// Plans that can share grouped launches: equal size and precision, and
-// separable real-space operators in both sub-steps (the grouped row kernels
+// Plans that can share grouped launches: equal size, precision and kernel
+// shapes, and separable real-space operators in both sub-steps (the grouped row kernels
 // carry the separable point-wise code).
 void build_groups(sgpe_batch* b) {
   std::vector<bool> taken(b->plans.size(), false);
@@ -1356,9 +1577,13 @@ void build_groups(sgpe_batch* b) {
     g.nx = p->nx;
     g.ny = p->ny;
     g.bits = p->bits;
+    g.row_shape = p->row_shape;
+    g.col_shape = p->col_shape;
     for (size_t k = i; k < b->plans.size(); ++k) {
       const sgpe_plan* q = b->plans[k];
-      if (!taken[k] && q->nx == p->nx && q->ny == p->ny && q->bits == p->bits && sep(q)) g.members.push_back(int(k));
+      if (!taken[k] && q->nx == p->nx && q->ny == p->ny && q->bits == p->bits && q->row_shape == p->row_shape &&
+          q->col_shape == p->col_shape && sep(q))
+        g.members.push_back(int(k));
     }
     if (g.members.size() < 2) continue;
     for (int k : g.members) taken[k] = true;

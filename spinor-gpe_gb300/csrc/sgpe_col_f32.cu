@@ -3,5 +3,5 @@
 #include "sgpe_launch.cuh"
 
 namespace sgpe {
-template cudaError_t launch_col<float>(const ColArgs<float>&, int, cudaStream_t);
+template cudaError_t launch_col_s<float, 0>(const ColArgs<float>&, int, cudaStream_t);
 }  // namespace sgpe

@@ -3,5 +3,5 @@
 #include "sgpe_launch.cuh"
 
 namespace sgpe {
-template cudaError_t launch_col<double>(const ColArgs<double>&, int, cudaStream_t);
+template cudaError_t launch_col_s<double, 0>(const ColArgs<double>&, int, cudaStream_t);
 }  // namespace sgpe

@@ -430,13 +430,43 @@ template <class C, int E, bool WARP = false, bool TC = false> struct LineSmem {
   C* base;
   int line_stride;
   TcScratch tc;
-  __device__ __forceinline__ C ld(int l, int i) const { return base[l * line_stride + i + i / E]; }
-  __device__ __forceinline__ void st(int l, int i, C v) const { base[l * line_stride + i + i / E] = v; }
+  // padded position of element i (i >= 0)
+  static __device__ __forceinline__ unsigned pad(unsigned i) { return i + i / unsigned(E); }
+  __device__ __forceinline__ C* line(int l) const { return base + l * line_stride; }
+  __device__ __forceinline__ C ld(int l, int i) const { return line(l)[pad(unsigned(i))]; }
+  __device__ __forceinline__ void st(int l, int i, C v) const { line(l)[pad(unsigned(i))] = v; }
   __device__ __forceinline__ void sync() const {
     if constexpr (WARP) __syncwarp();
     else __syncthreads();
   }
 };
+
+// Compile-time address folding for the exchanges.  A stage reads element
+// j + c (c = qT + r N/R) and writes element b(vt) + r NS; when the pad term
+// floor(i / E) of every such element differs from that of the base (j, or
+// b(vt)) by a constant for all threads, each access is the padded base plus
+// a compile-time offset.  These predicates check that exhaustively over the
+// threads of a line.
+__host__ __device__ constexpr int pad_div(int i, int e) { return i / e; }
+template <int N, int E, int R, int Q> __host__ __device__ constexpr bool loads_fold() {
+  constexpr int T = N / E;
+  for (int q = 0; q < Q; ++q)
+    for (int r = 0; r < R; ++r) {
+      const int c = q * T + r * (N / R);
+      const int d = pad_div(c, E);
+      for (int j = 1; j < T; ++j)
+        if (pad_div(j + c, E) - pad_div(j, E) != d) return false;
+    }
+  return true;
+}
+template <int N, int E, int R, int NS> __host__ __device__ constexpr bool stores_fold() {
+  for (int vt = 0; vt < N / R; ++vt) {
+    const int b = (vt / NS) * NS * R + (vt % NS);
+    for (int r = 1; r < R; ++r)
+      if (pad_div(b + r * NS, E) - pad_div(b, E) != pad_div(r * NS, E)) return false;
+  }
+  return true;
+}
 
 // One Stockham stage (and, recursively, the stages after it) on L lines.
 // FROM_SMEM: the first stage reads the natural-order line from shared memory
@@ -454,14 +484,22 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
   constexpr bool kLast = (NS * R == N);
   static_assert(E % R == 0, "radix must divide the points per thread");
   C a[L][Q][R];
+  constexpr bool kLdFold = loads_fold<N, E, R, Q>();
+  const unsigned pj = SM::pad(unsigned(j));
 #pragma unroll
   for (int l = 0; l < L; ++l)
 #pragma unroll
     for (int q = 0; q < Q; ++q)
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        if constexpr (kFirst && !FROM_SMEM) a[l][q][r] = v[l][q + r * Q];
-        else a[l][q][r] = sm.ld(l, j + q * T + r * (N / R));
+        if constexpr (kFirst && !FROM_SMEM) {
+          a[l][q][r] = v[l][q + r * Q];
+        } else if constexpr (kLdFold) {
+          const int c = q * T + r * (N / R);
+          a[l][q][r] = sm.line(l)[pj + unsigned(c + c / E)];
+        } else {
+          a[l][q][r] = sm.ld(l, j + q * T + r * (N / R));
+        }
       }
   if constexpr (!kFirst && SGPE_TW_FACTOR && Q > 1 && T * Q == NS) {
     // The Q butterflies of the thread sit at k = j + qT with NS = TQ, so
@@ -511,14 +549,21 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
         for (int r = 0; r < R; ++r) v[l][q + r * Q] = a[l][q][r];
   } else {
     sm.sync();  // earlier readers of the exchange buffer are done
+    constexpr bool kStFold = stores_fold<N, E, R, NS>();
 #pragma unroll
     for (int l = 0; l < L; ++l)
 #pragma unroll
       for (int q = 0; q < Q; ++q) {
         const int vt = j + q * T;
         const int base = (vt / NS) * NS * R + (vt % NS);
+        if constexpr (kStFold) {
+          C* sp = sm.line(l) + SM::pad(unsigned(base));
 #pragma unroll
-        for (int r = 0; r < R; ++r) sm.st(l, base + r * NS, a[l][q][r]);
+          for (int r = 0; r < R; ++r) sp[r * NS + (r * NS) / E] = a[l][q][r];
+        } else {
+#pragma unroll
+          for (int r = 0; r < R; ++r) sm.st(l, base + r * NS, a[l][q][r]);
+        }
       }
     if constexpr (!kLast) {
       sm.sync();

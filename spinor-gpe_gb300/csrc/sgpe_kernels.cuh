@@ -23,6 +23,19 @@
 // renormalisation (see ColArgs::norm_num).
 #pragma once
 #include "sgpe_fft.cuh"
+#include "sgpe_tma.cuh"
+
+// Row-pass lines through bulk asynchronous copies (TMA) for sides of at
+// least SGPE_ROW_TMA_MIN_N: 1 stages the input lines in shared memory,
+// 2 also writes the output lines from shared memory with bulk stores.
+// Measured on GB300 (1024^2 complex64 row pass): loads alone no change,
+// loads and stores 22.9 -> 21.8 us; at 256^2-512^2 both were slower.
+#ifndef SGPE_ROW_TMA
+#define SGPE_ROW_TMA 2
+#endif
+#ifndef SGPE_ROW_TMA_MIN_N
+#define SGPE_ROW_TMA_MIN_N 1024
+#endif
 
 // Unroll factor of the row kernel's point-wise loop (small: keeps the code
 // within the instruction cache).
@@ -33,6 +46,10 @@
 namespace sgpe {
 
 constexpr int kOpsUnroll = SGPE_OPS_UNROLL;
+
+// Device error word codes (a kernel that gives up a bounded wait records one
+// and carries on with plain loads).
+enum { kErrNone = 0, kErrCopyTimeout = 1 };
 
 // Programmatic dependent launch: the pass kernels are launched so that they
 // may start while the previous kernel in the stream is finishing.  Before
@@ -182,6 +199,8 @@ template <typename R> struct RowArgs {
   double atom_num;
   int tc;                 // launch the tensor-core DFT16 kernels (host side)
   const uint32_t* tcb;    // their B fragments (kTcBfragWords, device)
+  int shape;              // kernel shape of the launch (host side)
+  int* err;               // non-null: device error word (kErr* codes)
 };
 
 template <typename R> struct ColArgs {
@@ -200,6 +219,7 @@ template <typename R> struct ColArgs {
                           // pass sums them with (at least) FP64 accuracy
   int tc;                 // launch the tensor-core DFT16 kernels (host side)
   const uint32_t* tcb;    // their B fragments (kTcBfragWords, device)
+  int shape;              // kernel shape of the launch (host side)
 };
 
 template <typename R> struct ScaleArgs {
@@ -549,9 +569,47 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
 
   C v[1][E];
   const C* __restrict__ in = a.in[comp];
-  wait_for_previous_grid();
+  constexpr int kTma = N >= SGPE_ROW_TMA_MIN_N ? SGPE_ROW_TMA : 0;
+  bool staged = false;
+  if constexpr (kTma >= 1) {
+    // The block's 2*ROWS input lines are staged by bulk copies into the
+    // start of the exchange area (unpadded, line after line) when both
+    // components are 16-byte aligned (a line of N*sizeof(C) bytes always is
+    // a multiple of 16).
+    __shared__ __align__(8) uint64_t s_bar;
+    const bool tma = aligned16(a.in[0]) && aligned16(a.in[1]);
+    if (tma) {
+      if (tid == 0) mbar_init(&s_bar, 1);
+      __syncthreads();
+    }
+    wait_for_previous_grid();
+    if (tma) {
+      constexpr uint32_t kLine = N * sizeof(C);
+      if (tid == 0) {
+        mbar_arrive_expect_tx(&s_bar, 2 * ROWS * kLine);
 #pragma unroll
-  for (int m = 0; m < E; ++m) v[0][m] = ld_state(in + row_off + j + m * T);
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+          for (int r = 0; r < ROWS; ++r)
+            bulk_load(sm + (c * ROWS + r) * N, a.in[c] + (long long)(blockIdx.x * ROWS + r) * N, kLine, &s_bar);
+      }
+      staged = mbar_wait_bounded(&s_bar, 0);
+      if (staged) {
+        const C* line = sm + (comp * ROWS + rho) * N;
+#pragma unroll
+        for (int m = 0; m < E; ++m) v[0][m] = line[j + m * T];
+      } else if (a.err != nullptr) {
+        atomicExch(a.err, kErrCopyTimeout);
+      }
+      __syncthreads();  // the staged lines overlap the exchange lines
+    }
+  } else {
+    wait_for_previous_grid();
+  }
+  if (!staged) {
+#pragma unroll
+    for (int m = 0; m < E; ++m) v[0][m] = ld_state(in + row_off + j + m * T);
+  }
   allow_next_grid();
   // line (comp, rho) at sm + (comp*ROWS + rho)*LS; a line's T threads lie in
   // one warp when T divides 32 (the transforms then synchronise per warp)
@@ -582,6 +640,15 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
       const LineSmem<C, E> r0{sm + rho * LS, 0};
       const LineSmem<C, E> r1{sm + (ROWS + rho) * LS, 0};
       const int jj = tid % (2 * T);
+      // element x = jj + m*2T of each row: padded position pad(jj) + m*kStep
+      // when 2T is a multiple of E (every power-of-two plan)
+      using LS0 = LineSmem<C, E>;
+      constexpr bool kOpsFold = (2 * T) % E == 0;
+      constexpr int kStep = 2 * T + (2 * T) / E;
+      C* const q0 = r0.line(0) + LS0::pad(unsigned(jj));
+      C* const q1 = r1.line(0) + LS0::pad(unsigned(jj));
+      auto at0 = [&](int m, int x) -> C& { return kOpsFold ? q0[m * kStep] : r0.line(0)[LS0::pad(unsigned(x))]; };
+      auto at1 = [&](int m, int x) -> C& { return kOpsFold ? q1[m * kStep] : r1.line(0)[LS0::pad(unsigned(x))]; };
       if constexpr (SEP) {
         // separable operators: x-tables read at jj + m*2T (compile-time
         // offsets from one base), row values and the uniform c hoisted
@@ -596,7 +663,7 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
 #pragma unroll kOpsUnroll
         for (int m = 0; m < E / 2; ++m) {
           const int x = jj + m * 2 * T;
-          C p0 = cscale(r0.ld(0, x), lam), p1 = cscale(r1.ld(0, x), lam);
+          C p0 = cscale(at0(m, x), lam), p1 = cscale(at1(m, x), lam);
           v.pa0 = __ldg(pa0 + m * 2 * T);
           v.pa1 = __ldg(pa1 + m * 2 * T);
           if (a.coupling) {
@@ -604,8 +671,8 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
             v.s10 = __ldg(s10 + m * 2 * T);
           }
           apply_real_ops<R>(p0, p1, v, a);
-          r0.st(0, x, p0);
-          r1.st(0, x, p1);
+          at0(m, x) = p0;
+          at1(m, x) = p1;
         }
       } else {
         RowFields<R> rf;
@@ -613,10 +680,10 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
 #pragma unroll kOpsUnroll
         for (int m = 0; m < E / 2; ++m) {
           const int x = jj + m * 2 * T;
-          C p0 = cscale(r0.ld(0, x), lam), p1 = cscale(r1.ld(0, x), lam);
+          C p0 = cscale(at0(m, x), lam), p1 = cscale(at1(m, x), lam);
           real_space_ops<R>(p0, p1, x, rf, a);
-          r0.st(0, x, p0);
-          r1.st(0, x, p1);
+          at0(m, x) = p0;
+          at1(m, x) = p1;
         }
       }
     }
@@ -630,6 +697,26 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
     for (int m = 0; m < E; ++m) v[0][m] = cscale(v[0][m], a.scale);
   }
   C* out = a.out[comp];
+  if (kTma >= 2 && aligned16(a.out[0]) && aligned16(a.out[1])) {
+    // output lines through shared memory and bulk stores
+    constexpr uint32_t kLine = N * sizeof(C);
+    __syncthreads();  // the transform's last exchange has been read
+    C* line = sm + (comp * ROWS + rho) * N;
+#pragma unroll
+    for (int m = 0; m < E; ++m) line[j + m * T] = v[0][m];
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+      for (int c = 0; c < 2; ++c)
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r)
+          bulk_store(a.out[c] + (long long)(blockIdx.x * ROWS + r) * N, sm + (c * ROWS + r) * N, kLine);
+      bulk_commit();
+      bulk_wait_read();
+    }
+    return;
+  }
 #pragma unroll
   for (int m = 0; m < E; ++m) st_state(out + row_off + j + m * T, v[0][m]);
   (void)NT;

@@ -83,8 +83,42 @@ template <typename R> constexpr int pick_e(int n, int e_pow2) {
   return (n % 3 == 0) ? (n >= 768 ? Tune<R>::R3_E_LARGE : Tune<R>::R3_E) : cmin(n, e_pow2);
 }
 
-template <typename R, int N> struct RowCfg {
-  static constexpr int E = pick_e<R>(N, N >= 2048 ? Tune<R>::ROW_E_LARGE : Tune<R>::ROW_E);
+// Kernel shapes.  A pass over lines of one length can run in several
+// shapes: launch configurations that differ in points per thread E (and so in
+// the radix plan and the twiddle tables) and in lines per block.  Shape 0 is
+// the configuration chosen by Tune above; shapes 1 and 2, offered for
+// power-of-two sides up to kShapeMaxSide, take fewer points per thread, which
+// gives small grids more warps per SM for more transform stages.  Every shape
+// computes the same transform; the rounding differs with the radix plan.  A
+// plan picks one shape per axis (built-in defaults measured on GB300, or its
+// autotuner).
+constexpr int kMaxShapes = 3;
+constexpr int kShapeMaxSide = 512;
+template <typename R> struct ShapeTune;
+template <> struct ShapeTune<float> {
+  static constexpr int ROW_SHAPES = 3, COL_SHAPES = 3;
+  static constexpr int row_e(int s) { return s == 1 ? 8 : 4; }
+  static constexpr int col_e(int) { return 8; }
+  static constexpr int cols(int s) { return s == 2 ? 4 : Tune<float>::COLS; }
+};
+template <> struct ShapeTune<double> {
+  static constexpr int ROW_SHAPES = 2, COL_SHAPES = 2;
+  static constexpr int row_e(int) { return 4; }
+  static constexpr int col_e(int) { return 4; }
+  static constexpr int cols(int) { return Tune<double>::COLS; }
+};
+constexpr bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+template <typename R> constexpr int row_shape_count(int n) {
+  return (is_pow2(n) && n <= kShapeMaxSide) ? ShapeTune<R>::ROW_SHAPES : 1;
+}
+template <typename R> constexpr int col_shape_count(int n) {
+  return (is_pow2(n) && n <= kShapeMaxSide) ? ShapeTune<R>::COL_SHAPES : 1;
+}
+
+template <typename R, int N, int S = 0> struct RowCfg {
+  static constexpr bool VALID = S < row_shape_count<R>(N);
+  static constexpr int E = S == 0 ? pick_e<R>(N, N >= 2048 ? Tune<R>::ROW_E_LARGE : Tune<R>::ROW_E)
+                                  : cmin(N, ShapeTune<R>::row_e(S));
   static constexpr int T = N / E;
   // threads: 2 components x T per row; at least one warp, at most 16 rows
   static constexpr int ROWS = cmax(cmax(cmin(Tune<R>::ROW_THREADS / (2 * T), 16), 1), 32 / (2 * T));
@@ -95,10 +129,11 @@ template <typename R, int N> struct RowCfg {
                    1024 / THREADS));
 };
 
-template <typename R, int N> struct ColCfg {
-  static constexpr int E = pick_e<R>(N, Tune<R>::COL_E);
+template <typename R, int N, int S = 0> struct ColCfg {
+  static constexpr bool VALID = S < col_shape_count<R>(N);
+  static constexpr int E = S == 0 ? pick_e<R>(N, Tune<R>::COL_E) : cmin(N, ShapeTune<R>::col_e(S));
   static constexpr int T = N / E;
-  static constexpr int COLS = cmax(cmin(Tune<R>::COLS, 1024 / T), 32 / T);
+  static constexpr int COLS = cmax(cmin(S == 0 ? Tune<R>::COLS : ShapeTune<R>::cols(S), 1024 / T), 32 / T);
   static constexpr int THREADS = T * COLS;
   static constexpr size_t SMEM = size_t(COLS) * (N + N / E + 2) * sizeof(Cx<R>);
   static constexpr int MINB = cmax(
@@ -165,34 +200,42 @@ inline cudaError_t launch_pdl(K kernel, dim3 grid, dim3 block, size_t smem, cuda
 #endif
 }
 
-template <typename R, bool SEP> struct RowLauncher {
+template <typename R, bool SEP, int S> struct RowLauncher {
   const RowArgs<R>* a;
   int ny;
   cudaStream_t s;
   template <int N> cudaError_t run() const {
-    using Cfg = RowCfg<R, N>;
-    if (ny % Cfg::ROWS != 0) return cudaErrorInvalidValue;
-    auto k = row_kernel<R, N, Cfg::E, Cfg::ROWS, Cfg::MINB, SEP>;
-    static unsigned long long done = 0;
-    cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
-    if (e != cudaSuccess) return e;
-    return launch_pdl(k, dim3(ny / Cfg::ROWS), dim3(Cfg::THREADS), Cfg::SMEM, s, *a);
+    using Cfg = RowCfg<R, N, S>;
+    if constexpr (!Cfg::VALID) {
+      return cudaErrorInvalidValue;
+    } else {
+      if (ny % Cfg::ROWS != 0) return cudaErrorInvalidValue;
+      auto k = row_kernel<R, N, Cfg::E, Cfg::ROWS, Cfg::MINB, SEP>;
+      static unsigned long long done = 0;
+      cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
+      if (e != cudaSuccess) return e;
+      return launch_pdl(k, dim3(ny / Cfg::ROWS), dim3(Cfg::THREADS), Cfg::SMEM, s, *a);
+    }
   }
 };
 
-template <typename R> struct ColLauncher {
+template <typename R, int S> struct ColLauncher {
   const ColArgs<R>* a;
   int ny;
   cudaStream_t s;
   template <int N> cudaError_t run() const {
-    using Cfg = ColCfg<R, N>;
-    const int nx = a->nx;
-    if (nx % Cfg::COLS != 0 || (nx / 2) % Cfg::COLS != 0) return cudaErrorInvalidValue;
-    auto k = col_kernel<R, N, Cfg::E, Cfg::COLS, Cfg::MINB>;
-    static unsigned long long done = 0;
-    cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
-    if (e != cudaSuccess) return e;
-    return launch_pdl(k, dim3(nx / Cfg::COLS, 2), dim3(Cfg::THREADS), Cfg::SMEM, s, *a);
+    using Cfg = ColCfg<R, N, S>;
+    if constexpr (!Cfg::VALID) {
+      return cudaErrorInvalidValue;
+    } else {
+      const int nx = a->nx;
+      if (nx % Cfg::COLS != 0 || (nx / 2) % Cfg::COLS != 0) return cudaErrorInvalidValue;
+      auto k = col_kernel<R, N, Cfg::E, Cfg::COLS, Cfg::MINB>;
+      static unsigned long long done = 0;
+      cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
+      if (e != cudaSuccess) return e;
+      return launch_pdl(k, dim3(nx / Cfg::COLS, 2), dim3(Cfg::THREADS), Cfg::SMEM, s, *a);
+    }
   }
 };
 
@@ -289,94 +332,135 @@ inline int tc_col_tile_width(int ny) {
 
 // Grouped launches: G solves of the same size in one launch, per-solve
 // arguments in device memory (blockIdx.y / blockIdx.z selects the solve).
-template <typename R, bool SEP> struct RowGroupedLauncher {
+template <typename R, bool SEP, int S> struct RowGroupedLauncher {
   const RowArgs<R>* args;
   int groups, ny;
   cudaStream_t s;
   template <int N> cudaError_t run() const {
-    using Cfg = RowCfg<R, N>;
-    if (ny % Cfg::ROWS != 0) return cudaErrorInvalidValue;
-    auto k = row_kernel_grouped<R, N, Cfg::E, Cfg::ROWS, Cfg::MINB, SEP>;
-    static unsigned long long done = 0;
-    cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
-    if (e != cudaSuccess) return e;
-    return launch_pdl(k, dim3(ny / Cfg::ROWS, groups), dim3(Cfg::THREADS), Cfg::SMEM, s, args);
+    using Cfg = RowCfg<R, N, S>;
+    if constexpr (!Cfg::VALID) {
+      return cudaErrorInvalidValue;
+    } else {
+      if (ny % Cfg::ROWS != 0) return cudaErrorInvalidValue;
+      auto k = row_kernel_grouped<R, N, Cfg::E, Cfg::ROWS, Cfg::MINB, SEP>;
+      static unsigned long long done = 0;
+      cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
+      if (e != cudaSuccess) return e;
+      return launch_pdl(k, dim3(ny / Cfg::ROWS, groups), dim3(Cfg::THREADS), Cfg::SMEM, s, args);
+    }
   }
 };
 
-template <typename R> struct ColGroupedLauncher {
+template <typename R, int S> struct ColGroupedLauncher {
   const ColArgs<R>* args;
   int groups, nx;
   cudaStream_t s;
   template <int N> cudaError_t run() const {
-    using Cfg = ColCfg<R, N>;
-    if (nx % Cfg::COLS != 0 || (nx / 2) % Cfg::COLS != 0) return cudaErrorInvalidValue;
-    auto k = col_kernel_grouped<R, N, Cfg::E, Cfg::COLS, Cfg::MINB>;
-    static unsigned long long done = 0;
-    cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
-    if (e != cudaSuccess) return e;
-    return launch_pdl(k, dim3(nx / Cfg::COLS, 2, groups), dim3(Cfg::THREADS), Cfg::SMEM, s, args);
+    using Cfg = ColCfg<R, N, S>;
+    if constexpr (!Cfg::VALID) {
+      return cudaErrorInvalidValue;
+    } else {
+      if (nx % Cfg::COLS != 0 || (nx / 2) % Cfg::COLS != 0) return cudaErrorInvalidValue;
+      auto k = col_kernel_grouped<R, N, Cfg::E, Cfg::COLS, Cfg::MINB>;
+      static unsigned long long done = 0;
+      cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
+      if (e != cudaSuccess) return e;
+      return launch_pdl(k, dim3(nx / Cfg::COLS, 2, groups), dim3(Cfg::THREADS), Cfg::SMEM, s, args);
+    }
   }
 };
 
-template <typename R> struct ColsQuery {
-  int* out;
-  template <int N> cudaError_t run() const {
-    *out = ColCfg<R, N>::COLS;
-    return cudaSuccess;
-  }
-};
+// Per-shape launch functions, explicitly instantiated in their own
+// translation units (shape 0 with the default kernels, shapes 1-2 together).
+template <typename R, bool SEP, int S> cudaError_t launch_row_ops_s(const RowArgs<R>& a, int nx, int ny, cudaStream_t s) {
+  return dispatch_n(nx, RowLauncher<R, SEP, S>{&a, ny, s});
+}
+template <typename R, int S> cudaError_t launch_col_s(const ColArgs<R>& a, int ny, cudaStream_t s) {
+  return dispatch_n(ny, ColLauncher<R, S>{&a, ny, s});
+}
+template <typename R, int S>
+cudaError_t launch_row_grouped_s(const RowArgs<R>* args, int groups, int nx, int ny, cudaStream_t s) {
+  return dispatch_n(nx, RowGroupedLauncher<R, true, S>{args, groups, ny, s});
+}
+template <typename R, int S>
+cudaError_t launch_col_grouped_s(const ColArgs<R>* args, int groups, int nx, int ny, cudaStream_t s) {
+  return dispatch_n(ny, ColGroupedLauncher<R, S>{args, groups, nx, s});
+}
 
-// Row kernels with the separable (SEP) or the generic point-wise code.
+#define SGPE_SHAPE_SWITCH(shape, CALL0, CALL1, CALL2) \
+  switch (shape) {                                   \
+    case 0: return CALL0;                            \
+    case 1: return CALL1;                            \
+    case 2: return CALL2;                            \
+    default: return cudaErrorInvalidValue;           \
+  }
+
+// Row kernels with the separable (SEP) or the generic point-wise code, in
+// the shape a.shape.
 template <typename R, bool SEP> cudaError_t launch_row_ops(const RowArgs<R>& a, int nx, int ny, cudaStream_t s) {
-  return dispatch_n(nx, RowLauncher<R, SEP>{&a, ny, s});
+  SGPE_SHAPE_SWITCH(a.shape, (launch_row_ops_s<R, SEP, 0>(a, nx, ny, s)), (launch_row_ops_s<R, SEP, 1>(a, nx, ny, s)),
+                    (launch_row_ops_s<R, SEP, 2>(a, nx, ny, s)))
 }
 
 template <typename R> cudaError_t launch_col(const ColArgs<R>& a, int ny, cudaStream_t s) {
   if (a.tc) return launch_col_tc(a, ny, s);
-  return dispatch_n(ny, ColLauncher<R>{&a, ny, s});
+  SGPE_SHAPE_SWITCH(a.shape, (launch_col_s<R, 0>(a, ny, s)), (launch_col_s<R, 1>(a, ny, s)),
+                    (launch_col_s<R, 2>(a, ny, s)))
 }
 
-// `args` in device memory, `groups` solves of an (ny, nx) grid.
-template <typename R> cudaError_t launch_row_grouped(const RowArgs<R>* args, int groups, int nx, int ny,
-                                                     cudaStream_t s) {
-  return dispatch_n(nx, RowGroupedLauncher<R, true>{args, groups, ny, s});
+// `args` in device memory, `groups` solves of an (ny, nx) grid, all in the
+// kernel shape `shape`.
+template <typename R>
+cudaError_t launch_row_grouped(const RowArgs<R>* args, int shape, int groups, int nx, int ny, cudaStream_t s) {
+  SGPE_SHAPE_SWITCH(shape, (launch_row_grouped_s<R, 0>(args, groups, nx, ny, s)),
+                    (launch_row_grouped_s<R, 1>(args, groups, nx, ny, s)),
+                    (launch_row_grouped_s<R, 2>(args, groups, nx, ny, s)))
 }
-template <typename R> cudaError_t launch_col_grouped(const ColArgs<R>* args, int groups, int nx, int ny,
-                                                     cudaStream_t s) {
-  return dispatch_n(ny, ColGroupedLauncher<R>{args, groups, nx, s});
+template <typename R>
+cudaError_t launch_col_grouped(const ColArgs<R>* args, int shape, int groups, int nx, int ny, cudaStream_t s) {
+  SGPE_SHAPE_SWITCH(shape, (launch_col_grouped_s<R, 0>(args, groups, nx, ny, s)),
+                    (launch_col_grouped_s<R, 1>(args, groups, nx, ny, s)),
+                    (launch_col_grouped_s<R, 2>(args, groups, nx, ny, s)))
 }
 
-template <typename R> struct RowEQuery {
-  int* out;
+// Per-shape geometry queries (0 if the size or shape is unsupported).
+template <typename R, int S> struct ShapeQuery {
+  int* row_e;
+  int* col_e;
+  int* cols;
   template <int N> cudaError_t run() const {
-    *out = RowCfg<R, N>::E;
+    if constexpr (RowCfg<R, N, S>::VALID) *row_e = RowCfg<R, N, S>::E;
+    if constexpr (ColCfg<R, N, S>::VALID) {
+      *col_e = ColCfg<R, N, S>::E;
+      *cols = ColCfg<R, N, S>::COLS;
+    }
     return cudaSuccess;
   }
 };
-template <typename R> struct ColEQuery {
-  int* out;
-  template <int N> cudaError_t run() const {
-    *out = ColCfg<R, N>::E;
-    return cudaSuccess;
+template <typename R> void shape_geometry(int n, int shape, int* row_e, int* col_e, int* cols) {
+  *row_e = *col_e = *cols = 0;
+  switch (shape) {
+    case 0: dispatch_n(n, ShapeQuery<R, 0>{row_e, col_e, cols}); break;
+    case 1: dispatch_n(n, ShapeQuery<R, 1>{row_e, col_e, cols}); break;
+    case 2: dispatch_n(n, ShapeQuery<R, 2>{row_e, col_e, cols}); break;
+    default: break;
   }
-};
-// Points per thread of the row (x) and column (y) transforms (0 if unsupported).
-template <typename R> int row_points_per_thread(int nx) {
-  int e = 0;
-  if (dispatch_n(nx, RowEQuery<R>{&e}) != cudaSuccess) return 0;
-  return e;
 }
-template <typename R> int col_points_per_thread(int ny) {
-  int e = 0;
-  if (dispatch_n(ny, ColEQuery<R>{&e}) != cudaSuccess) return 0;
-  return e;
+// Points per thread of the row (x) and column (y) transforms.
+template <typename R> int row_points_per_thread(int nx, int shape = 0) {
+  int re, ce, c;
+  shape_geometry<R>(nx, shape, &re, &ce, &c);
+  return re;
 }
-
-// Column-tile width used for a column length ny (0 if unsupported).
-template <typename R> int col_tile_width(int ny) {
-  int c = 0;
-  if (dispatch_n(ny, ColsQuery<R>{&c}) != cudaSuccess) return 0;
+template <typename R> int col_points_per_thread(int ny, int shape = 0) {
+  int re, ce, c;
+  shape_geometry<R>(ny, shape, &re, &ce, &c);
+  return ce;
+}
+// Column-tile width used for a column length ny.
+template <typename R> int col_tile_width(int ny, int shape = 0) {
+  int re, ce, c;
+  shape_geometry<R>(ny, shape, &re, &ce, &c);
   return c;
 }
 
@@ -400,16 +484,19 @@ template <typename R> cudaError_t launch_copy(const CopyArgs<R>& a, cudaStream_t
 // The kernels are instantiated in separate translation units (one per
 // precision and pass) so the build compiles them in parallel.
 #ifndef SGPE_INSTANTIATE
-extern template cudaError_t launch_row_ops<float, true>(const RowArgs<float>&, int, int, cudaStream_t);
-extern template cudaError_t launch_row_ops<float, false>(const RowArgs<float>&, int, int, cudaStream_t);
-extern template cudaError_t launch_row_ops<double, true>(const RowArgs<double>&, int, int, cudaStream_t);
-extern template cudaError_t launch_row_ops<double, false>(const RowArgs<double>&, int, int, cudaStream_t);
-extern template cudaError_t launch_col<float>(const ColArgs<float>&, int, cudaStream_t);
-extern template cudaError_t launch_col<double>(const ColArgs<double>&, int, cudaStream_t);
-extern template cudaError_t launch_row_grouped<float>(const RowArgs<float>*, int, int, int, cudaStream_t);
-extern template cudaError_t launch_row_grouped<double>(const RowArgs<double>*, int, int, int, cudaStream_t);
-extern template cudaError_t launch_col_grouped<float>(const ColArgs<float>*, int, int, int, cudaStream_t);
-extern template cudaError_t launch_col_grouped<double>(const ColArgs<double>*, int, int, int, cudaStream_t);
+#define SGPE_EXTERN_SHAPE(R, S)                                                                                  \
+  extern template cudaError_t launch_row_ops_s<R, true, S>(const RowArgs<R>&, int, int, cudaStream_t);            \
+  extern template cudaError_t launch_row_ops_s<R, false, S>(const RowArgs<R>&, int, int, cudaStream_t);           \
+  extern template cudaError_t launch_col_s<R, S>(const ColArgs<R>&, int, cudaStream_t);                           \
+  extern template cudaError_t launch_row_grouped_s<R, S>(const RowArgs<R>*, int, int, int, cudaStream_t);         \
+  extern template cudaError_t launch_col_grouped_s<R, S>(const ColArgs<R>*, int, int, int, cudaStream_t);
+SGPE_EXTERN_SHAPE(float, 0)
+SGPE_EXTERN_SHAPE(float, 1)
+SGPE_EXTERN_SHAPE(float, 2)
+SGPE_EXTERN_SHAPE(double, 0)
+SGPE_EXTERN_SHAPE(double, 1)
+SGPE_EXTERN_SHAPE(double, 2)
+#undef SGPE_EXTERN_SHAPE
 #endif
 
 // Row pass: the separable kernels unless the step uses generic operator

@@ -3,5 +3,5 @@
 #include "sgpe_launch.cuh"
 
 namespace sgpe {
-template cudaError_t launch_row_ops<float, true>(const RowArgs<float>&, int, int, cudaStream_t);
+template cudaError_t launch_row_ops_s<float, true, 0>(const RowArgs<float>&, int, int, cudaStream_t);
 }  // namespace sgpe

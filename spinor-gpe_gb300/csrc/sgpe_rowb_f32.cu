@@ -3,5 +3,5 @@
 #include "sgpe_launch.cuh"
 
 namespace sgpe {
-template cudaError_t launch_row_grouped<float>(const RowArgs<float>*, int, int, int, cudaStream_t);
+template cudaError_t launch_row_grouped_s<float, 0>(const RowArgs<float>*, int, int, int, cudaStream_t);
 }  // namespace sgpe

@@ -3,5 +3,5 @@
 #include "sgpe_launch.cuh"
 
 namespace sgpe {
-template cudaError_t launch_row_grouped<double>(const RowArgs<double>*, int, int, int, cudaStream_t);
+template cudaError_t launch_row_grouped_s<double, 0>(const RowArgs<double>*, int, int, int, cudaStream_t);
 }  // namespace sgpe

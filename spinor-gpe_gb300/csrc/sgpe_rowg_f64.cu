@@ -3,5 +3,5 @@
 #include "sgpe_launch.cuh"
 
 namespace sgpe {
-template cudaError_t launch_row_ops<double, false>(const RowArgs<double>&, int, int, cudaStream_t);
+template cudaError_t launch_row_ops_s<double, false, 0>(const RowArgs<double>&, int, int, cudaStream_t);
 }  // namespace sgpe

@@ -28,7 +28,11 @@ EXPORTED = ('sgpe_version', 'sgpe_last_error', 'sgpe_plan_create',
             'sgpe_fft2_static', 'sgpe_set_energy_fields', 'sgpe_energy',
             'sgpe_batch_create', 'sgpe_batch_destroy', 'sgpe_batch_steps',
             'sgpe_set_dft_mode', 'sgpe_analysis', 'sgpe_setup_spinor',
-            'sgpe_imprint_vortices', 'sgpe_fourier_split_x')
+            'sgpe_imprint_vortices', 'sgpe_fourier_split_x',
+            'sgpe_shape_count', 'sgpe_set_shapes', 'sgpe_get_shapes',
+            'sgpe_autotune')
+
+SGPE_MAX_SHAPES = 3
 
 
 class SgpeError(RuntimeError):
@@ -87,6 +91,13 @@ _SIGS = {
     'sgpe_batch_destroy': ([_VP], ctypes.c_int),
     'sgpe_batch_steps': ([_VP, ctypes.c_int, _VP], ctypes.c_int),
     'sgpe_set_dft_mode': ([_VP, ctypes.c_int], ctypes.c_int),
+    'sgpe_shape_count': ([ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    'sgpe_set_shapes': ([_VP, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    'sgpe_get_shapes': ([_VP, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
+                        ctypes.c_int),
+    'sgpe_autotune': ([_VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                       ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double), _VP],
+                      ctypes.c_int),
     'sgpe_analysis': ([_VP] + [_VP] * 10 + [_VP, _VP], ctypes.c_int),
     'sgpe_setup_spinor': ([ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP,
                            ctypes.c_double, _VP, ctypes.c_double, ctypes.c_ulonglong,
@@ -176,6 +187,29 @@ class Plan:
     def set_dft_mode(self, mode):
         """0: FP32 radix-16 DFTs; 1: split-BF16 tensor-core DFT16."""
         check(load().sgpe_set_dft_mode(self._h, int(mode)))
+
+    def set_shapes(self, row_shape, col_shape):
+        """Kernel shapes of the row and column passes (keeps the state)."""
+        check(load().sgpe_set_shapes(self._h, int(row_shape), int(col_shape)))
+
+    @property
+    def shapes(self):
+        """Current (row shape, column shape)."""
+        r, c = ctypes.c_int(), ctypes.c_int()
+        check(load().sgpe_get_shapes(self._h, ctypes.byref(r), ctypes.byref(c)))
+        return r.value, c.value
+
+    def autotune(self, torch, n_steps, device):
+        """Time every pair of kernel shapes over n_steps steps from the
+        current state and keep the fastest; returns ((row, col), {(row,
+        col): microseconds per step}).  The state is unchanged."""
+        r, c = ctypes.c_int(), ctypes.c_int()
+        us = (ctypes.c_double * (SGPE_MAX_SHAPES * SGPE_MAX_SHAPES))()
+        check(load().sgpe_autotune(self._h, int(n_steps), ctypes.byref(r),
+                                   ctypes.byref(c), us, _stream(torch, device)))
+        times = {(i // SGPE_MAX_SHAPES, i % SGPE_MAX_SHAPES): us[i]
+                 for i in range(SGPE_MAX_SHAPES * SGPE_MAX_SHAPES) if us[i] > 0}
+        return (r.value, c.value), times
 
     def set_physics(self, g_uu, g_dd, g_ud, atom_num, dv_r, dv_k,
                     is_coupling):

@@ -25,6 +25,7 @@ Differences a caller can observe:
 import numpy as np
 import torch
 
+from .. import tuning
 from . import _native
 from . import operators as ops
 from . import prop_result
@@ -120,13 +121,17 @@ class TensorPropagator:
     ``PSpinor``), ``t_step``, ``n_steps``, ``device``, ``time`` ('imag' or
     'real'), ``is_sampling``, ``n_samples``; plus ``dtype`` (64 / 128) and
     ``tensor_core_dft`` (complex64 only: radix-16 DFT stages as split-BF16
-    products on the tensor cores, a precision-study variant).
+    products on the tensor cores, a precision-study variant),
+    ``kernel_shapes`` (row and column kernel shapes, default: the shapes
+    remembered for this grid by ``spinor_gpe.tuning``, else the library's
+    built-in defaults) and ``autotune`` (time every pair of shapes on the
+    initial state and keep the fastest, see ``autotune()``).
     """
 
     # pylint: disable=too-many-instance-attributes
     def __init__(self, spin, t_step, n_steps, device='cuda', time='imag',
                  is_sampling=False, n_samples=1, dtype=128,
-                 tensor_core_dft=False):
+                 tensor_core_dft=False, kernel_shapes=None, autotune=False):
         self.n_steps = n_steps
         self._device = cuda_device(device)
         self.device = device
@@ -189,6 +194,10 @@ class TensorPropagator:
         self.tensor_core_dft = bool(tensor_core_dft)
         if self.tensor_core_dft:
             self._plan.set_dft_mode(1)
+        elif kernel_shapes is not None:
+            self._plan.set_shapes(*kernel_shapes)
+        elif tuning.lookup(self._bits, ny, nx) is not None:
+            self._plan.set_shapes(*tuning.lookup(self._bits, ny, nx))
         dv_r = float(self._space_np['dv_r'])
         dv_k = float(self._space_np['dv_k'])
         self._plan.set_physics(float(self.g_sc['uu']), float(self.g_sc['dd']),
@@ -210,6 +219,9 @@ class TensorPropagator:
         self._psik_cache = None
         self.psik = [torch.as_tensor(p, dtype=self._ctype, device=self._device)
                      for p in psik0]
+        self.tune_times = None
+        if autotune and not self.tensor_core_dft:
+            self.autotune()
 
     # ------------------------------------------------------------ attributes
     @property
@@ -286,6 +298,29 @@ class TensorPropagator:
             raise ValueError('t_step does not match the operators passed')
         self._plan.single_step(torch, sub, self._device)
         self._psik_cache = None
+
+    @property
+    def kernel_shapes(self):
+        """(row shape, column shape) of the plan's pass kernels."""
+        return self._plan.shapes
+
+    @kernel_shapes.setter
+    def kernel_shapes(self, shapes):
+        self._plan.set_shapes(*shapes)
+
+    def autotune(self, n_steps=None):
+        """Time ``n_steps`` full steps (default ``tuning.default_steps``) in
+        every pair of kernel shapes, each from the current state, and keep
+        the fastest; the state is unchanged.  The choice is remembered for
+        this grid (``spinor_gpe.tuning``).  Returns {(row, col): microseconds
+        per step}, also kept as ``tune_times``."""
+        ny, nx = self._shape
+        if n_steps is None:
+            n_steps = tuning.default_steps(ny, nx)
+        shapes, times = self._plan.autotune(torch, n_steps, self._device)
+        tuning.remember(self._bits, ny, nx, shapes)
+        self.tune_times = times
+        return times
 
     def full_steps(self, n_steps, pops=None):
         """``n_steps`` full steps in one call; ``pops`` is an optional

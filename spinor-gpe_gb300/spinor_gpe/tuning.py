@@ -1,0 +1,68 @@
+"""Kernel-shape wisdom: the shapes the autotuner picked, per grid.
+
+Every pass of the solver (the row pass along x and the column pass along y)
+can run in several kernel shapes (launch configurations with different
+points per thread and radix plans; ``sgpe_shape_count`` in
+``include/spinor_gb300.h``).  A new plan starts in built-in defaults
+measured on GB300; ``TensorPropagator.autotune()`` times every pair of
+shapes on the live state and keeps the fastest (``sgpe_autotune``).  The
+choices are remembered here per (precision bits, ny, nx) for the rest of the
+process, so later propagators of the same grid start in them, and can be
+saved to and loaded from a JSON file (like FFTW's wisdom).  When the
+environment variable ``SGPE_WISDOM`` names a readable file it is loaded at
+import.
+
+Shapes change the rounding of the transforms (every shape meets the parity
+tolerances), so a run is reproducible bit for bit only with the same
+shapes; the wisdom file records them.
+"""
+import json
+import os
+
+_WISDOM = {}
+
+
+def _key(bits, ny, nx):
+    return (int(bits), int(ny), int(nx))
+
+
+def remember(bits, ny, nx, shapes):
+    """Record the (row, column) shapes for a grid."""
+    _WISDOM[_key(bits, ny, nx)] = (int(shapes[0]), int(shapes[1]))
+
+
+def lookup(bits, ny, nx):
+    """The remembered (row, column) shapes of a grid, or None."""
+    return _WISDOM.get(_key(bits, ny, nx))
+
+
+def forget():
+    """Drop all remembered shapes (new plans take the built-in defaults)."""
+    _WISDOM.clear()
+
+
+def save(path):
+    """Write the remembered shapes as JSON."""
+    rows = [{'bits': k[0], 'ny': k[1], 'nx': k[2], 'row_shape': v[0],
+             'col_shape': v[1]} for k, v in sorted(_WISDOM.items())]
+    with open(path, 'w', encoding='utf-8') as f:
+        json.dump({'kernel_shapes': rows}, f, indent=1)
+
+
+def load(path):
+    """Merge shapes from a JSON file written by ``save``."""
+    with open(path, encoding='utf-8') as f:
+        data = json.load(f)
+    for r in data.get('kernel_shapes', []):
+        remember(r['bits'], r['ny'], r['nx'], (r['row_shape'], r['col_shape']))
+
+
+def default_steps(ny, nx):
+    """Steps per candidate for ``autotune``: about 2e7 grid-point steps,
+    between 16 and 256."""
+    return int(max(16, min(256, 2e7 // (int(ny) * int(nx)))))
+
+
+_ENV = os.environ.get('SGPE_WISDOM')
+if _ENV and os.path.isfile(_ENV):
+    load(_ENV)

@@ -254,6 +254,12 @@ int sgpe_set_dft_mode(sgpe_plan* plan, int mode);
  * is unsupported.  sgpe_set_shapes: switch the plan's shapes (new twiddle
  * tables, graphs re-captured; the state is kept; the tensor-core DFT mode
  * runs shape 0 only).  sgpe_get_shapes: the current shapes. */
+/* Device error word of the plan's pass kernels: 0, or 1 when a kernel gave
+ * up a bounded wait for its bulk (TMA) copies and continued with plain loads
+ * (the state of that pass is not reliable).  Synchronous (a 4-byte device
+ * read); returns SGPE_ERR_CUDA with a message when the word is non-zero. */
+int sgpe_device_status(sgpe_plan* plan, int* status);
+
 #define SGPE_MAX_SHAPES 3
 int sgpe_shape_count(int dtype_bits, int axis, int n);
 int sgpe_set_shapes(sgpe_plan* plan, int row_shape, int col_shape);

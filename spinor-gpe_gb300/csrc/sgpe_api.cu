@@ -16,6 +16,9 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "sgpe_analysis.cuh"
 #include "sgpe_energy.cuh"
 #include "sgpe_launch.cuh"
@@ -146,6 +149,9 @@ struct sgpe_plan {
   void* epsi[2] = {nullptr, nullptr};   // real-space spinor for the energy
   double* epart = nullptr;              // energy block partials [2][kEnergyBlocks][6]
   double* apart = nullptr;              // analysis block partials
+  void* tmaps = nullptr;     // two CUtensorMap of the state (column-pass tiles)
+  bool tmaps_valid = false;  // encoded for the current column shape
+  int* derr = nullptr;       // device error word (bounded waits that gave up)
   double g[3] = {0, 0, 0};
   double atom_num = 1.0, dv_r = 1.0, dv_k = 1.0;
   int coupling = 0;
@@ -262,6 +268,20 @@ int shape_count(int bits, int axis, int n) {
   if (!sgpe::size_supported(n)) return 0;
   if (bits == 64) return axis == 0 ? sgpe::row_shape_count<float>(n) : sgpe::col_shape_count<float>(n);
   return axis == 0 ? sgpe::row_shape_count<double>(n) : sgpe::col_shape_count<double>(n);
+}
+
+// cuTensorMapEncodeTiled from the driver, looked up once through the
+// runtime (no link-time dependency on libcuda); null if unavailable.
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  return fn;
 }
 
 void free_sub(SubOps& so) {
@@ -520,6 +540,8 @@ template <typename R> bool col_step_args(sgpe_plan* p, int sub, bool want_u, sgp
   a.tc = p->tc;
   a.tcb = p->tcb;
   a.shape = p->col_shape;
+  a.tmap = (p->tmaps_valid && !p->tc) ? p->tmaps : nullptr;  // in place, no shifts
+  a.err = p->derr;
   a.nx = p->nx;
   a.fwd = (p->form == kMixed);
   a.inv = 1;
@@ -557,6 +579,7 @@ template <typename R> sgpe::RowArgs<R> row_step_args(sgpe_plan* p, int sub, doub
   a.tc = p->tc;
   a.tcb = p->tcb;
   a.shape = p->row_shape;
+  a.err = p->derr;
   a.mode = sgpe::kRowStep;
   a.scale = R(1);
   a.part = reinterpret_cast<R*>(p->part);
@@ -751,6 +774,36 @@ int energy_impl(sgpe_plan* p, int slot, const void* k0, const void* k1, double* 
   return e == cudaSuccess ? SGPE_OK : cuda_fail(e, "energy (finalise)");
 }
 
+// Tensor maps of the two state components for the column pass's TMA tiles
+// (ColArgs::tmap): the component as a 2-D array of working-precision
+// scalars {2 nx, ny} (row stride nx complex values), box {2 COLS, min(ny,
+// 256)} for the current column shape.  Left invalid (plain loads) when the
+// encoder is unavailable or refuses the layout.
+template <typename R> void update_col_tmaps(sgpe_plan* p) {
+  p->tmaps_valid = false;
+  if (!SGPE_COL_TMA) return;  // the kernels are built without the TMA tiles
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  const int cols = sgpe::col_tile_width<R>(p->ny, p->col_shape);
+  if (enc == nullptr || cols == 0) return;
+  if (p->tmaps == nullptr && cudaMalloc(&p->tmaps, 2 * sizeof(CUtensorMap)) != cudaSuccess) {
+    p->tmaps = nullptr;
+    return;
+  }
+  CUtensorMap maps[2];
+  const cuuint64_t dims[2] = {cuuint64_t(2) * p->nx, cuuint64_t(p->ny)};
+  const cuuint64_t strides[1] = {cuuint64_t(p->nx) * p->elem};
+  const cuuint32_t box[2] = {cuuint32_t(2 * cols), cuuint32_t(std::min(p->ny, 256))};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUtensorMapDataType dt = sizeof(R) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  for (int c = 0; c < 2; ++c)
+    if (enc(&maps[c], dt, 2, p->s[c], dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return;
+  if (cudaMemcpy(p->tmaps, maps, sizeof(maps), cudaMemcpyHostToDevice) != cudaSuccess) return;
+  p->tmaps_valid = true;
+}
+
 void drop_graphs(sgpe_plan* p) {
   ++p->epoch;
   for (auto& g : p->graph) {
@@ -834,6 +887,7 @@ template <typename R> int apply_shapes(sgpe_plan* p, int rs, int cs) {
   p->col_shape = cs;
   p->ntile_fp32 = p->nx / cols;
   p->ntile = p->ntile_fp32;
+  update_col_tmaps<R>(p);
   return SGPE_OK;
 }
 
@@ -923,10 +977,14 @@ int sgpe_plan_create(sgpe_plan** out, int ny, int nx, int dtype_bits, int device
         p->tw_y = upload_twiddles<double>(ny, sgpe::col_points_per_thread<double>(ny, p->col_shape), &e);
     }
   }
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&p->derr), sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(p->derr, 0, sizeof(int));
   if (e != cudaSuccess) {
     sgpe_plan_destroy(p);
     return fail(SGPE_ERR_OOM, std::string("plan allocation: ") + cudaGetErrorString(e));
   }
+  if (dtype_bits == 64) update_col_tmaps<float>(p);
+  else update_col_tmaps<double>(p);
   *out = p;
   return SGPE_OK;
 }
@@ -954,6 +1012,8 @@ int sgpe_plan_destroy(sgpe_plan* p) {
   if (p->epart) cudaFree(p->epart);
   if (p->tcb) cudaFree(p->tcb);
   if (p->apart) cudaFree(p->apart);
+  if (p->tmaps) cudaFree(p->tmaps);
+  if (p->derr) cudaFree(p->derr);
   delete p;
   return SGPE_OK;
 }
@@ -1323,6 +1383,18 @@ int sgpe_time_passes(sgpe_plan* p, int n_steps, double* col_ms, double* row_ms, 
   if (e != cudaSuccess) return cuda_fail(e, "time_passes");
   *col_ms = tc / n_pass;
   *row_ms = tr / n_pass;
+  return SGPE_OK;
+}
+
+int sgpe_device_status(sgpe_plan* p, int* status) {
+  if (p == nullptr || status == nullptr) return fail(SGPE_ERR_ARG, "null plan or status");
+  DeviceGuard g(p->device);
+  int h = 0;
+  const cudaError_t e = cudaMemcpy(&h, p->derr, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "device status");
+  *status = h;
+  if (h != 0) return fail(SGPE_ERR_CUDA, "a pass kernel gave up waiting for its bulk copies (device error word " +
+                                             std::to_string(h) + "); results of that pass are not reliable");
   return SGPE_OK;
 }
 

@@ -29,12 +29,26 @@
 // least SGPE_ROW_TMA_MIN_N: 1 stages the input lines in shared memory,
 // 2 also writes the output lines from shared memory with bulk stores.
 // Measured on GB300 (1024^2 complex64 row pass): loads alone no change,
-// loads and stores 22.9 -> 21.8 us; at 256^2-512^2 both were slower.
+// loads and stores 22.9 -> 21.8 us before the exchange addressing was
+// folded, a tie (21.3 us) after; at 256^2-512^2 both were slower.
 #ifndef SGPE_ROW_TMA
 #define SGPE_ROW_TMA 2
 #endif
 #ifndef SGPE_ROW_TMA_MIN_N
 #define SGPE_ROW_TMA_MIN_N 1024
+#endif
+// Column-pass tiles (COLS columns x N rows) through 2-D tensor copies (TMA
+// loads into shared memory on an mbarrier, TMA stores back) for column
+// lengths of at least SGPE_COL_TMA_MIN_N, when the host passes tensor maps
+// (in-place steady-state passes).  Off by default: measured on GB300 the
+// column pass took 19.4 -> 20.3 us at 1024^2 and 62.6 -> 69.0 us at 2048^2
+// with it (the block waits for its whole tile either way; one thread's
+// copies replace the 16 strided loads per thread but not the wait).
+#ifndef SGPE_COL_TMA
+#define SGPE_COL_TMA 0
+#endif
+#ifndef SGPE_COL_TMA_MIN_N
+#define SGPE_COL_TMA_MIN_N 512
 #endif
 
 // Unroll factor of the row kernel's point-wise loop (small: keeps the code
@@ -220,6 +234,10 @@ template <typename R> struct ColArgs {
   int tc;                 // launch the tensor-core DFT16 kernels (host side)
   const uint32_t* tcb;    // their B fragments (kTcBfragWords, device)
   int shape;              // kernel shape of the launch (host side)
+  // non-null: two 2-D tensor maps (128 bytes each, device memory) of the
+  // components, in == out, no shifts; box {2 COLS scalars, min(N, 256) rows}
+  const void* tmap;
+  int* err;               // non-null: device error word (kErr* codes)
 };
 
 template <typename R> struct ScaleArgs {
@@ -764,11 +782,52 @@ __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
   C* out = a.out[comp];
 
   C v[1][E];
-  wait_for_previous_grid();
+  // TMA staging of the block's tile: rows of COLS complex values, row-major,
+  // at a 128-byte aligned start of the exchange area
+  constexpr bool kTma = SGPE_COL_TMA && N >= SGPE_COL_TMA_MIN_N;
+  constexpr int kBoxY = N < 256 ? N : 256;
+  constexpr uint32_t kTileBytes = uint32_t(COLS) * N * sizeof(C);
+  static_assert(!kTma || sizeof(C) * COLS * (N / E + 2) >= 128, "the aligned tile must fit the exchange area");
+  static_assert(!kTma || (COLS * sizeof(C)) % 16 == 0, "tile rows must be whole 16-byte units");
+  C* const stage = reinterpret_cast<C*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  const char* const tmap = static_cast<const char*>(a.tmap) + comp * 128;
+  bool staged = false;
+  if constexpr (kTma) {
+    __shared__ __align__(8) uint64_t s_bar;
+    const bool tma = a.tmap != nullptr;
+    if (tma) {
+      if (tid == 0) {
+        mbar_init(&s_bar, 1);
+        prefetch_tensormap(tmap);
+      }
+      __syncthreads();
+    }
+    wait_for_previous_grid();
+    if (tma) {
+      if (tid == 0) {
+        mbar_arrive_expect_tx(&s_bar, kTileBytes);
 #pragma unroll
-  for (int m = 0; m < E; ++m) {
-    const int row = j + (a.in_shift ? (m + E / 2) % E : m) * T;
-    v[0][m] = ld_state(in + (long long)row * nx + xin);
+        for (int b = 0; b < N / kBoxY; ++b)
+          tensor_load_2d(stage + b * kBoxY * COLS, tmap, blockIdx.x * COLS * 2, b * kBoxY, &s_bar);
+      }
+      staged = mbar_wait_bounded(&s_bar, 0);
+      if (staged) {
+#pragma unroll
+        for (int m = 0; m < E; ++m) v[0][m] = stage[(j + m * T) * COLS + c];
+      } else if (a.err != nullptr) {
+        atomicExch(a.err, kErrCopyTimeout);
+      }
+      __syncthreads();  // the tile overlaps the exchange lines
+    }
+  } else {
+    wait_for_previous_grid();
+  }
+  if (!staged) {
+#pragma unroll
+    for (int m = 0; m < E; ++m) {
+      const int row = j + (a.in_shift ? (m + E / 2) % E : m) * T;
+      v[0][m] = ld_state(in + (long long)row * nx + xin);
+    }
   }
   allow_next_grid();
   const LineSmem<C, E, false, TC> smv{sm + c * LS, 0, tcs};
@@ -787,10 +846,26 @@ __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
 #pragma unroll
     for (int m = 0; m < E; ++m) v[0][m] = cscale(v[0][m], a.scale);
   }
+  if (kTma && a.tmap != nullptr) {
+    // the tile back through shared memory and tensor stores (in place)
+    __syncthreads();  // the transform's last exchange has been read
 #pragma unroll
-  for (int m = 0; m < E; ++m) {
-    const int row = j + (a.out_shift ? (m + E / 2) % E : m) * T;
-    st_state(out + (long long)row * nx + xout, v[0][m]);
+    for (int m = 0; m < E; ++m) stage[(j + m * T) * COLS + c] = v[0][m];
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+      for (int b = 0; b < N / kBoxY; ++b)
+        tensor_store_2d(tmap, blockIdx.x * COLS * 2, b * kBoxY, stage + b * kBoxY * COLS);
+      bulk_commit();
+      bulk_wait_read();
+    }
+  } else {
+#pragma unroll
+    for (int m = 0; m < E; ++m) {
+      const int row = j + (a.out_shift ? (m + E / 2) % E : m) * T;
+      st_state(out + (long long)row * nx + xout, v[0][m]);
+    }
   }
   if (a.part != nullptr) {
     su = warp_sum(su);

@@ -30,7 +30,7 @@ EXPORTED = ('sgpe_version', 'sgpe_last_error', 'sgpe_plan_create',
             'sgpe_set_dft_mode', 'sgpe_analysis', 'sgpe_setup_spinor',
             'sgpe_imprint_vortices', 'sgpe_fourier_split_x',
             'sgpe_shape_count', 'sgpe_set_shapes', 'sgpe_get_shapes',
-            'sgpe_autotune')
+            'sgpe_autotune', 'sgpe_device_status')
 
 SGPE_MAX_SHAPES = 3
 
@@ -92,6 +92,7 @@ _SIGS = {
     'sgpe_batch_steps': ([_VP, ctypes.c_int, _VP], ctypes.c_int),
     'sgpe_set_dft_mode': ([_VP, ctypes.c_int], ctypes.c_int),
     'sgpe_shape_count': ([ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    'sgpe_device_status': ([_VP, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
     'sgpe_set_shapes': ([_VP, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     'sgpe_get_shapes': ([_VP, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
                         ctypes.c_int),
@@ -187,6 +188,11 @@ class Plan:
     def set_dft_mode(self, mode):
         """0: FP32 radix-16 DFTs; 1: split-BF16 tensor-core DFT16."""
         check(load().sgpe_set_dft_mode(self._h, int(mode)))
+
+    def check_device_status(self):
+        """Raise if a pass kernel recorded a failed bounded wait."""
+        st = ctypes.c_int()
+        check(load().sgpe_device_status(self._h, ctypes.byref(st)))
 
     def set_shapes(self, row_shape, col_shape):
         """Kernel shapes of the row and column passes (keeps the state)."""

@@ -299,6 +299,11 @@ class TensorPropagator:
         self._plan.single_step(torch, sub, self._device)
         self._psik_cache = None
 
+    def check_device(self):
+        """Raise ``SgpeError`` if a pass kernel gave up a bounded wait for
+        its bulk copies since the plan was created (synchronous)."""
+        self._plan.check_device_status()
+
     @property
     def kernel_shapes(self):
         """(row shape, column shape) of the plan's pass kernels."""
@@ -380,6 +385,7 @@ class TensorPropagator:
                    for k, v in self.analysis(psi_t, psik_t).items()}
         psik = ttools.to_numpy(psik_t)
         psi = ttools.to_numpy(psi_t)
+        self.check_device()
         return prop_result.PropResult(psi, psik, energy, pops, file_name,
                                       derived=derived)
 

@@ -66,3 +66,50 @@ def default_steps(ny, nx):
 _ENV = os.environ.get('SGPE_WISDOM')
 if _ENV and os.path.isfile(_ENV):
     load(_ENV)
+
+
+def tune_grids(sides, bits=64, time='real', n_steps=None, device='cuda'):
+    """Autotune square grids of the given sides on the Raman-dressed
+    workload (harmonic trap, Omega = 1, k_L = 3, delta = 0.5; the set-up of
+    ``workloads.raman_quench_1024`` scaled to each side) and remember the
+    choices.  Returns {side: {(row, col): microseconds per step}}."""
+    import tempfile
+
+    from . import workloads
+    from .pspinor import pspinor as spin
+    from .pspinor import tensor_propagator as tprop
+    from .pspinor import tensor_tools as ttools
+    out = {}
+    for n in sides:
+        path = tempfile.mkdtemp(prefix='sgpe_tune_') + '/q/'
+        ps = workloads.raman_quench_1024(spin.PSpinor, ttools.fft_2d, path, n=int(n), delta=0.5)
+        dt = 1e-3 if time == 'real' else 0.02
+        prop = tprop.TensorPropagator(ps, dt, 10, device, time=time, dtype=bits)
+        prop.full_steps(2)
+        out[int(n)] = prop.autotune(n_steps=n_steps or max(32, default_steps(n, n)))
+    return out
+
+
+def _main(argv=None):
+    import argparse
+    ap = argparse.ArgumentParser(
+        prog='python -m spinor_gpe.tuning',
+        description='Autotune the kernel shapes of square grids on this GPU, print the '
+                    'step times of every pair and optionally save the choices as wisdom.')
+    ap.add_argument('--sides', type=int, nargs='+', default=[32, 64, 128, 256, 512])
+    ap.add_argument('--dtype', type=int, choices=(64, 128), default=64)
+    ap.add_argument('--time', choices=('real', 'imag'), default='real')
+    ap.add_argument('--steps', type=int, default=None, help='steps per candidate')
+    ap.add_argument('--out', default=None, help='write the wisdom JSON here')
+    a = ap.parse_args(argv)
+    res = tune_grids(a.sides, a.dtype, a.time, a.steps)
+    for n, times in res.items():
+        best = lookup(a.dtype, n, n)
+        cells = ', '.join(f'({r},{c}) {us:.1f}' for (r, c), us in sorted(times.items()))
+        print(f'complex{a.dtype} {n}x{n} {a.time}: us/step {cells}; kept {best}')
+    if a.out:
+        save(a.out)
+
+
+if __name__ == '__main__':
+    _main()

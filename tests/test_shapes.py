@@ -87,7 +87,8 @@ def _c128_twin(name):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize('name', ['imag_raman_64x32', 'real_rot_32x64', 'real_raman_32_c64',
-                                  'imag_plain_32_c64', 'imag_gradients_32'])
+                                  'imag_plain_32_c64', 'imag_gradients_32', 'real_bump_32',
+                                  'imag_raman_64'])
 def test_every_shape_matches_reference(tp, tmp_path, name):
     case = CASES[name]
     p = case_params(case)
@@ -250,3 +251,34 @@ def test_batch_in_other_shapes_matches_solves_alone(tp, tmp_path):
     for a, b in zip(alone, together):
         np.testing.assert_array_equal(_psik(a), _psik(b))
     batch.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('bits', [64, 128])
+def test_fft_every_shape_matches_numpy(tp, bits):
+    """The plan's centred 2-D transforms in every pair of shapes (non-square
+    grid, both directions) against NumPy."""
+    import torch
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    ny, nx = 256, 128
+    rng = np.random.default_rng(3)
+    a = [rng.standard_normal((ny, nx)) + 1j * rng.standard_normal((ny, nx)) for _ in range(2)]
+    dr = (0.125, 0.25)
+    ref_k = ttools.fft_2d(a, dr)
+    ref_r = ttools.ifft_2d(a, dr)
+    norm = dr[0] * dr[1] / (2 * np.pi)
+    dt = torch.complex64 if bits == 64 else torch.complex128
+    t = [torch.as_tensor(x, dtype=dt, device='cuda') for x in a]
+    plan = _native.Plan(ny, nx, bits, torch.cuda.current_device())
+    tol = 2e-6 if bits == 64 else 1e-14
+    try:
+        for shapes in _pairs(bits, ny, nx):
+            plan.set_shapes(*shapes)
+            assert plan.shapes == shapes
+            out = [torch.empty_like(x) for x in t]
+            plan.fft2(torch, t, out, False, norm)
+            assert rel_l2([o.cpu().numpy() for o in out], ref_k) <= tol, shapes
+            plan.fft2(torch, t, out, True, 1.0 / (ny * nx * norm))
+            assert rel_l2([o.cpu().numpy() for o in out], ref_r) <= tol, shapes
+    finally:
+        plan.close()

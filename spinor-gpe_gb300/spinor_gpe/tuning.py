@@ -102,13 +102,18 @@ def _main(argv=None):
     ap.add_argument('--steps', type=int, default=None, help='steps per candidate')
     ap.add_argument('--out', default=None, help='write the wisdom JSON here')
     a = ap.parse_args(argv)
-    res = tune_grids(a.sides, a.dtype, a.time, a.steps)
+    # the propagators record their choices in the package's module (under
+    # ``python -m`` this file also runs as ``__main__``, a second copy)
+    from spinor_gpe import tuning as mod
+    res = mod.tune_grids(a.sides, a.dtype, a.time, a.steps)
     for n, times in res.items():
-        best = lookup(a.dtype, n, n)
+        if not times:
+            print(f'complex{a.dtype} {n}x{n} {a.time}: one kernel shape per pass at this side')
+            continue
         cells = ', '.join(f'({r},{c}) {us:.1f}' for (r, c), us in sorted(times.items()))
-        print(f'complex{a.dtype} {n}x{n} {a.time}: us/step {cells}; kept {best}')
+        print(f'complex{a.dtype} {n}x{n} {a.time}: us/step {cells}; kept {mod.lookup(a.dtype, n, n)}')
     if a.out:
-        save(a.out)
+        mod.save(a.out)
 
 
 if __name__ == '__main__':

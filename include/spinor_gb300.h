@@ -260,6 +260,12 @@ int sgpe_set_dft_mode(sgpe_plan* plan, int mode);
  * read); returns SGPE_ERR_CUDA with a message when the word is non-zero. */
 int sgpe_device_status(sgpe_plan* plan, int* status);
 
+/* Check of the bounded wait itself, on the current device: one block waits
+ * on an mbarrier phase that no copy completes; gave_up = 1 when every
+ * thread ended its wait by the limit (about 0.5 s, returned in waited_ms)
+ * instead of hanging.  No counterpart in the original. */
+int sgpe_check_bounded_wait(int* gave_up, double* waited_ms);
+
 #define SGPE_MAX_SHAPES 3
 int sgpe_shape_count(int dtype_bits, int axis, int n);
 int sgpe_set_shapes(sgpe_plan* plan, int row_shape, int col_shape);

@@ -1026,6 +1026,29 @@ namespace {
 __global__ void __launch_bounds__(256) tc_bfrag_kernel(uint32_t* bfrag) {
   sgpe::tc_fill_bfrag(bfrag, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
+
+// One block waits, with the pass kernels' bounded wait, on an mbarrier phase
+// that expects 16 bytes no copy will deliver; out[0] = 1 if every thread
+// gave up, out[1] = the nanoseconds thread 0 waited.
+__global__ void __launch_bounds__(64) wait_check_kernel(unsigned long long* out) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int gave_up;
+  if (threadIdx.x == 0) {
+    gave_up = 0;
+    sgpe::mbar_init(&bar, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) sgpe::mbar_arrive_expect_tx(&bar, 16);
+  const unsigned long long t0 = sgpe::global_ns();
+  const bool done = sgpe::mbar_wait_bounded(&bar, 0);
+  const unsigned long long t1 = sgpe::global_ns();
+  if (!done) atomicAdd(&gave_up, 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    out[0] = gave_up == int(blockDim.x) ? 1ull : 0ull;
+    out[1] = t1 - t0;
+  }
+}
 }  // namespace
 
 extern "C" {
@@ -1385,6 +1408,22 @@ int sgpe_time_passes(sgpe_plan* p, int n_steps, double* col_ms, double* row_ms, 
   if (e != cudaSuccess) return cuda_fail(e, "time_passes");
   *col_ms = tc / n_pass;
   *row_ms = tr / n_pass;
+  return SGPE_OK;
+}
+
+int sgpe_check_bounded_wait(int* gave_up, double* waited_ms) {
+  if (gave_up == nullptr || waited_ms == nullptr) return fail(SGPE_ERR_ARG, "null output");
+  unsigned long long* d = nullptr;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&d), 2 * sizeof(unsigned long long));
+  if (e != cudaSuccess) return cuda_fail(e, "bounded-wait check");
+  unsigned long long h[2] = {0, 0};
+  wait_check_kernel<<<1, 64>>>(d);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(e, "bounded-wait check");
+  *gave_up = int(h[0]);
+  *waited_ms = double(h[1]) * 1e-6;
   return SGPE_OK;
 }
 

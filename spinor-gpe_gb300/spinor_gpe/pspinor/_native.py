@@ -30,7 +30,7 @@ EXPORTED = ('sgpe_version', 'sgpe_last_error', 'sgpe_plan_create',
             'sgpe_set_dft_mode', 'sgpe_analysis', 'sgpe_setup_spinor',
             'sgpe_imprint_vortices', 'sgpe_fourier_split_x',
             'sgpe_shape_count', 'sgpe_set_shapes', 'sgpe_get_shapes',
-            'sgpe_autotune', 'sgpe_device_status')
+            'sgpe_autotune', 'sgpe_device_status', 'sgpe_check_bounded_wait')
 
 SGPE_MAX_SHAPES = 3
 
@@ -93,6 +93,8 @@ _SIGS = {
     'sgpe_set_dft_mode': ([_VP, ctypes.c_int], ctypes.c_int),
     'sgpe_shape_count': ([ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     'sgpe_device_status': ([_VP, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+    'sgpe_check_bounded_wait': ([ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)],
+                                ctypes.c_int),
     'sgpe_set_shapes': ([_VP, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     'sgpe_get_shapes': ([_VP, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
                         ctypes.c_int),

@@ -72,6 +72,9 @@ def parse():
     ap.add_argument('--tensor-core-dft', action='store_true',
                     help='raman_quench: run the split-BF16 tensor-core DFT16 '
                          'variant (precision study; not the headline)')
+    ap.add_argument('--kernel-shapes', type=int, nargs=2, default=None, metavar=('ROW', 'COL'),
+                    help='raman_quench: run the solves in these kernel shapes instead of the '
+                         'defaults (sgpe_shape_count lists them)')
     ap.add_argument('--host-setup', action='store_true',
                     help='served: build each request with the host PSpinor '
                          'set-up instead of the device set-up')
@@ -270,8 +273,10 @@ def run_native(args, world, rank, local):
     n_rep = max(1, math.ceil(2 * L2_BYTES / state_bytes) + 1)
     psik_host = [torch.as_tensor(np.asarray(p), dtype=torch.complex64)
                  .pin_memory() for p in ps.psik]
+    shapes = tuple(args.kernel_shapes) if args.kernel_shapes else None
     props = [tprop.TensorPropagator(ps, 1e-3, args.steps, device, time='real',
-                                    dtype=64, tensor_core_dft=args.tensor_core_dft)
+                                    dtype=64, tensor_core_dft=args.tensor_core_dft,
+                                    kernel_shapes=shapes)
              for _ in range(n_rep)]
     stream = torch.cuda.current_stream()
 
@@ -356,6 +361,7 @@ def run_native(args, world, rank, local):
                    'time': 'real', 'dt': 1e-3, 'delta': 0.5, 'omega': 1.0,
                    'k_L': 3.0, 'g': [1000.0, 1000.0, 990.0],
                    'replicas_per_gpu': n_rep,
+                   'kernel_shapes': list(props[0].kernel_shapes),
                    'l2': f'inputs larger than L2: {n_rep} replica states of '
                          f'{state_bytes >> 20} MiB stepped round-robin',
                    'parallelism': f'replicas x{world}'},

@@ -87,46 +87,50 @@ template <typename R> constexpr int pick_e(int n, int e_pow2) {
 // shapes: launch configurations that differ in points per thread E (and so in
 // the radix plan and the twiddle tables) and in lines per block.  Shape 0 is
 // the configuration chosen by Tune above; shapes 1 and 2, offered for
-// power-of-two sides up to kShapeMaxSide, take fewer points per thread, which
-// gives small grids more warps per SM for more transform stages.  Every shape
+// power-of-two sides up to 512, take fewer points per thread, which gives
+// small grids more warps per SM for more transform stages (ShapeTune).  Every shape
 // computes the same transform; the rounding differs with the radix plan.  A
 // plan picks one shape per axis (built-in defaults measured on GB300, or its
 // autotuner).
 constexpr int kMaxShapes = 3;
-constexpr int kShapeMaxSide = 512;
+constexpr bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 template <typename R> struct ShapeTune;
 template <> struct ShapeTune<float> {
-  static constexpr int ROW_SHAPES = 3, COL_SHAPES = 3;
-  static constexpr int row_e(int s) { return s == 1 ? 8 : 4; }
+  // rows: 8 / 4 points per thread up to 512; at 1024 one alternative with
+  // 32 points per thread (two radix-32 stages, warp-synchronous lines,
+  // 128 registers)
+  static constexpr int row_shapes(int n) { return !is_pow2(n) ? 1 : n <= 512 ? 3 : n == 1024 ? 2 : 1; }
+  static constexpr int col_shapes(int n) { return (is_pow2(n) && n <= 512) ? 3 : 1; }
+  static constexpr int row_e(int n, int s) { return n == 1024 ? 32 : s == 1 ? 8 : 4; }
+  static constexpr int row_minb(int n, int) { return n == 1024 ? 4 : 0; }  // 0: the shape-0 rule
   static constexpr int col_e(int) { return 8; }
   static constexpr int cols(int s) { return s == 2 ? 4 : Tune<float>::COLS; }
 };
 template <> struct ShapeTune<double> {
-  static constexpr int ROW_SHAPES = 2, COL_SHAPES = 2;
-  static constexpr int row_e(int) { return 4; }
+  static constexpr int row_shapes(int n) { return (is_pow2(n) && n <= 512) ? 2 : 1; }
+  static constexpr int col_shapes(int n) { return (is_pow2(n) && n <= 512) ? 2 : 1; }
+  static constexpr int row_e(int, int) { return 4; }
+  static constexpr int row_minb(int, int) { return 0; }
   static constexpr int col_e(int) { return 4; }
   static constexpr int cols(int) { return Tune<double>::COLS; }
 };
-constexpr bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
-template <typename R> constexpr int row_shape_count(int n) {
-  return (is_pow2(n) && n <= kShapeMaxSide) ? ShapeTune<R>::ROW_SHAPES : 1;
-}
-template <typename R> constexpr int col_shape_count(int n) {
-  return (is_pow2(n) && n <= kShapeMaxSide) ? ShapeTune<R>::COL_SHAPES : 1;
-}
+template <typename R> constexpr int row_shape_count(int n) { return ShapeTune<R>::row_shapes(n); }
+template <typename R> constexpr int col_shape_count(int n) { return ShapeTune<R>::col_shapes(n); }
 
 template <typename R, int N, int S = 0> struct RowCfg {
   static constexpr bool VALID = S < row_shape_count<R>(N);
   static constexpr int E = S == 0 ? pick_e<R>(N, N >= 2048 ? Tune<R>::ROW_E_LARGE : Tune<R>::ROW_E)
-                                  : cmin(N, ShapeTune<R>::row_e(S));
+                                  : cmin(N, ShapeTune<R>::row_e(N, S));
   static constexpr int T = N / E;
   // threads: 2 components x T per row; at least one warp, at most 16 rows
   static constexpr int ROWS = cmax(cmax(cmin(Tune<R>::ROW_THREADS / (2 * T), 16), 1), 32 / (2 * T));
   static constexpr int THREADS = 2 * T * ROWS;
   static constexpr size_t SMEM = 2ull * ROWS * (N + N / E) * sizeof(Cx<R>);
-  static constexpr int MINB =
-      cmax(1, cmin(N % 3 == 0 ? Tune<R>::R3_ROW_MINB : N >= 2048 ? Tune<R>::ROW_MINB_LARGE : Tune<R>::ROW_MINB,
-                   1024 / THREADS));
+  static constexpr int MINB_RULE =
+      (S > 0 && ShapeTune<R>::row_minb(N, S) > 0)
+          ? ShapeTune<R>::row_minb(N, S)
+          : (N % 3 == 0 ? Tune<R>::R3_ROW_MINB : N >= 2048 ? Tune<R>::ROW_MINB_LARGE : Tune<R>::ROW_MINB);
+  static constexpr int MINB = cmax(1, cmin(MINB_RULE, 1024 / THREADS));
 };
 
 template <typename R, int N, int S = 0> struct ColCfg {

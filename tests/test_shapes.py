@@ -34,7 +34,9 @@ def test_shape_counts(native_lib):
     lib = _native.load()
     assert lib.sgpe_shape_count(64, 0, 512) == 3
     assert lib.sgpe_shape_count(64, 1, 32) == 3
-    assert lib.sgpe_shape_count(64, 0, 1024) == 1
+    assert lib.sgpe_shape_count(64, 0, 1024) == 2
+    assert lib.sgpe_shape_count(64, 1, 1024) == 1
+    assert lib.sgpe_shape_count(64, 0, 2048) == 1
     assert lib.sgpe_shape_count(64, 0, 768) == 1
     assert lib.sgpe_shape_count(128, 0, 256) == 2
     assert lib.sgpe_shape_count(128, 1, 2048) == 1
@@ -148,6 +150,24 @@ def test_raman_512_complex64_every_shape(tp, tmp_path):
     n = 3
     ref = _oracle(ps, 1e-3, 'real', n)
     for shapes in _pairs(64, 512, 512):
+        prop = tp.TensorPropagator(ps, 1e-3, n, 'cuda', time='real', dtype=64, kernel_shapes=shapes)
+        prop.full_steps(n)
+        assert rel_l2(_psik(prop), ref) <= 1e-5, shapes
+
+
+@pytest.mark.gpu
+def test_raman_1024_complex64_every_shape(tp, tmp_path):
+    """1024^2 complex64: the radix-32 row shape against the oracle."""
+    from spinor_gpe import workloads
+    from spinor_gpe.pspinor import pspinor as spin
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    ps = workloads.raman_quench_1024(spin.PSpinor, ttools.fft_2d, str(tmp_path / 'q') + '/',
+                                     n=1024, delta=0.5)
+    n = 3
+    ref = _oracle(ps, 1e-3, 'real', n)
+    pairs = _pairs(64, 1024, 1024)
+    assert len(pairs) == 2
+    for shapes in pairs:
         prop = tp.TensorPropagator(ps, 1e-3, n, 'cuda', time='real', dtype=64, kernel_shapes=shapes)
         prop.full_steps(n)
         assert rel_l2(_psik(prop), ref) <= 1e-5, shapes

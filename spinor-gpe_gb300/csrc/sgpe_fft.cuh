@@ -425,19 +425,28 @@ __host__ __device__ constexpr int tw_offset(int N, int E, int NS) {
 // exchange between stages needs only a warp barrier.
 // TC: radix-16 stages take their DFT16 on the tensor cores (split-BF16,
 // sgpe_tc.cuh) with the staging area in `tc`.
+// bar > 0 (and !WARP): the line's threads are whole warps, and the
+// exchanges synchronise only them, on named barrier `bar` of `bar_threads`
+// threads, so lines of one block do not wait for each other.
 template <class C, int E, bool WARP = false, bool TC = false> struct LineSmem {
   static constexpr bool kTc = TC;
   C* base;
   int line_stride;
   TcScratch tc;
+  int bar = 0;
+  int bar_threads = 0;
   // padded position of element i (i >= 0)
   static __device__ __forceinline__ unsigned pad(unsigned i) { return i + i / unsigned(E); }
   __device__ __forceinline__ C* line(int l) const { return base + l * line_stride; }
   __device__ __forceinline__ C ld(int l, int i) const { return line(l)[pad(unsigned(i))]; }
   __device__ __forceinline__ void st(int l, int i, C v) const { line(l)[pad(unsigned(i))] = v; }
   __device__ __forceinline__ void sync() const {
-    if constexpr (WARP) __syncwarp();
-    else __syncthreads();
+    if constexpr (WARP) {
+      __syncwarp();
+    } else {
+      if (bar > 0) asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(bar_threads) : "memory");
+      else __syncthreads();
+    }
   }
 };
 

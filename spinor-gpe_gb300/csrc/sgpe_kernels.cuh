@@ -34,6 +34,14 @@
 #ifndef SGPE_ROW_TMA
 #define SGPE_ROW_TMA 2
 #endif
+// Row-pass exchanges synchronise each line's own warps (named barriers)
+// instead of the whole block.  Off: measured on GB300 the 1024^2 row pass
+// took 21.4 -> 25.5 us with it (the two component lines drift apart and the
+// block-wide barrier of the point-wise step waits for the later one),
+// 2048^2 63.8 -> 62.7 us.
+#ifndef SGPE_ROW_LINE_BARRIERS
+#define SGPE_ROW_LINE_BARRIERS 0
+#endif
 #ifndef SGPE_ROW_TMA_MIN_N
 #define SGPE_ROW_TMA_MIN_N 1024
 #endif
@@ -631,7 +639,11 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
   allow_next_grid();
   // line (comp, rho) at sm + (comp*ROWS + rho)*LS; a line's T threads lie in
   // one warp when T divides 32 (the transforms then synchronise per warp)
-  const LineSmem<C, E, (32 % T == 0), TC> smv{sm + (comp * ROWS + rho) * LS, 0, tcs};
+  // lines of T >= 32 threads are whole warps: each synchronises its own
+  // exchanges on named barrier 1 + line (SGPE_ROW_LINE_BARRIERS)
+  constexpr bool kLineBar = SGPE_ROW_LINE_BARRIERS && (T % 32 == 0) && (2 * ROWS <= 15);
+  const LineSmem<C, E, (32 % T == 0), TC> smv{sm + (comp * ROWS + rho) * LS, 0, tcs,
+                                              kLineBar ? 1 + comp * ROWS + rho : 0, kLineBar ? T : 0};
 
   if (a.mode == kRowStep) {
     // inverse x transform, result left in shared memory (natural order)

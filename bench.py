@@ -75,6 +75,9 @@ def parse():
     ap.add_argument('--kernel-shapes', type=int, nargs=2, default=None, metavar=('ROW', 'COL'),
                     help='raman_quench: run the solves in these kernel shapes instead of the '
                          'defaults (sgpe_shape_count lists them)')
+    ap.add_argument('--no-batch-autotune', action='store_true',
+                    help='batched_uneven: keep every solve in its default kernel shapes '
+                         '(no PropagatorBatch.autotune)')
     ap.add_argument('--host-setup', action='store_true',
                     help='served: build each request with the host PSpinor '
                          'set-up instead of the device set-up')
@@ -447,6 +450,17 @@ def run_batched(args, world, rank, local):
                                  'batched_us': 1e6 * t_grp}
 
     batch = PropagatorBatch(props)
+    tuned = None
+    if not args.no_batch_autotune:
+        # kernel shapes per size class for grouped stepping (set-up, untimed)
+        t0 = time.perf_counter()
+        tuned = batch.autotune()
+        tune_s = time.perf_counter() - t0
+        if breakdown is not None:
+            for (_, _, nx), times in tuned.items():
+                shapes = props[[p._shape[1] for p in props].index(nx)].kernel_shapes
+                breakdown[str(nx)]['batched_tuned_us'] = times[shapes]
+                breakdown[str(nx)]['tuned_shapes'] = list(shapes)
     batch.full_steps(max(args.warmup, 9))
     with ClockSampler(local) as clk:
         t_bat = timed(lambda: batch.full_steps(k))
@@ -474,8 +488,13 @@ def run_batched(args, world, rank, local):
                    'parallelism': f'replicas x{world}'},
         'sequential_plain': {'value': seq, 'unit': 'grid-point-steps/s',
                              'what': 'the same solves, each advanced alone '
-                                     'with TensorPropagator.full_steps'},
+                                     'with TensorPropagator.full_steps (default '
+                                     'kernel shapes)'},
         'speedup_vs_sequential': value / seq,
+        'batch_kernel_shapes': (None if tuned is None else {
+            f'{ny}x{nx}': list(props[[p._shape for p in props].index((ny, nx))].kernel_shapes)
+            for (_, ny, nx) in tuned}),
+        'batch_autotune_s': None if tuned is None else tune_s,
         'gpu_launches': 6 * k * args.solves,
         'per_class_step_us': breakdown,
         'clocks': clk.summary(),

@@ -98,21 +98,24 @@ template <typename R> struct ShapeTune;
 template <> struct ShapeTune<float> {
   // rows: 8 / 4 points per thread up to 512; at 1024 one alternative with
   // 32 points per thread (two radix-32 stages, warp-synchronous lines,
-  // 128 registers)
-  static constexpr int row_shapes(int n) { return !is_pow2(n) ? 1 : n <= 512 ? 3 : n == 1024 ? 2 : 1; }
-  static constexpr int col_shapes(int n) { return (is_pow2(n) && n <= 512) ? 3 : 1; }
-  static constexpr int row_e(int n, int s) { return n == 1024 ? 32 : s == 1 ? 8 : 4; }
+  // 128 registers); sides 3 * 2^k: the other multiple of 3 (12 <-> 24)
+  static constexpr int r3_alt(int n) { return n >= 768 ? 12 : 24; }
+  static constexpr int row_shapes(int n) {
+    return n % 3 == 0 ? 2 : !is_pow2(n) ? 1 : n <= 512 ? 3 : n == 1024 ? 2 : 1;
+  }
+  static constexpr int col_shapes(int n) { return n % 3 == 0 ? 2 : (is_pow2(n) && n <= 512) ? 3 : 1; }
+  static constexpr int row_e(int n, int s) { return n % 3 == 0 ? r3_alt(n) : n == 1024 ? 32 : s == 1 ? 8 : 4; }
   static constexpr int row_minb(int n, int) { return n == 1024 ? 4 : 0; }  // 0: the shape-0 rule
-  static constexpr int col_e(int) { return 8; }
-  static constexpr int cols(int s) { return s == 2 ? 4 : Tune<float>::COLS; }
+  static constexpr int col_e(int n, int) { return n % 3 == 0 ? r3_alt(n) : 8; }
+  static constexpr int cols(int n, int s) { return (n % 3 != 0 && s == 2) ? 4 : Tune<float>::COLS; }
 };
 template <> struct ShapeTune<double> {
   static constexpr int row_shapes(int n) { return (is_pow2(n) && n <= 512) ? 2 : 1; }
   static constexpr int col_shapes(int n) { return (is_pow2(n) && n <= 512) ? 2 : 1; }
   static constexpr int row_e(int, int) { return 4; }
   static constexpr int row_minb(int, int) { return 0; }
-  static constexpr int col_e(int) { return 4; }
-  static constexpr int cols(int) { return Tune<double>::COLS; }
+  static constexpr int col_e(int, int) { return 4; }
+  static constexpr int cols(int, int) { return Tune<double>::COLS; }
 };
 template <typename R> constexpr int row_shape_count(int n) { return ShapeTune<R>::row_shapes(n); }
 template <typename R> constexpr int col_shape_count(int n) { return ShapeTune<R>::col_shapes(n); }
@@ -135,9 +138,9 @@ template <typename R, int N, int S = 0> struct RowCfg {
 
 template <typename R, int N, int S = 0> struct ColCfg {
   static constexpr bool VALID = S < col_shape_count<R>(N);
-  static constexpr int E = S == 0 ? pick_e<R>(N, Tune<R>::COL_E) : cmin(N, ShapeTune<R>::col_e(S));
+  static constexpr int E = S == 0 ? pick_e<R>(N, Tune<R>::COL_E) : cmin(N, ShapeTune<R>::col_e(N, S));
   static constexpr int T = N / E;
-  static constexpr int COLS = cmax(cmin(S == 0 ? Tune<R>::COLS : ShapeTune<R>::cols(S), 1024 / T), 32 / T);
+  static constexpr int COLS = cmax(cmin(S == 0 ? Tune<R>::COLS : ShapeTune<R>::cols(N, S), 1024 / T), 32 / T);
   static constexpr int THREADS = T * COLS;
   static constexpr size_t SMEM = size_t(COLS) * (N + N / E + 2) * sizeof(Cx<R>);
   static constexpr int MINB = cmax(

@@ -7,6 +7,8 @@ the solves' steps are captured once as independent branches of a CUDA graph,
 so small solves that cannot fill the GPU alone run concurrently.  Each
 propagator stays usable on its own (``psik``, ``energy()``, ...).
 """
+import itertools
+
 import torch
 
 from .pspinor import _native
@@ -30,6 +32,59 @@ class PropagatorBatch:
         self._batch.steps(torch, n_steps, self._device)
         for p in self.propagators:
             p._psik_cache = None
+
+    def autotune(self, n_steps=32, warmup=9, margin=0.02):
+        """Kernel shapes for batched stepping, picked by measurement.
+
+        Solves of one precision and grid form a class; each class is stepped
+        as a batch of its own in every pair of kernel shapes
+        (``sgpe_shape_count``) and its solves take the fastest pair (their
+        current pair stays unless another is more than ``margin`` faster).
+        A class that runs as one grouped launch can prefer other shapes than
+        one solve alone (more blocks per launch favour more points per
+        thread).  The states are restored afterwards by reloading each
+        solve's psik, so stepping continues as from newly built propagators
+        with these shapes.  Returns {(bits, ny, nx): {(row, col): us per
+        class step}} for the classes that had a choice."""
+        lib = _native.load()
+        saved = [[t.clone() for t in p.psik] for p in self.propagators]
+        classes = {}
+        for p in self.propagators:
+            classes.setdefault((p._bits,) + tuple(p._shape), []).append(p)
+        out = {}
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        for key, members in classes.items():
+            bits, ny, nx = key
+            pairs = list(itertools.product(range(lib.sgpe_shape_count(bits, 0, nx)),
+                                           range(lib.sgpe_shape_count(bits, 1, ny))))
+            if len(pairs) < 2 or any(p.tensor_core_dft for p in members):
+                continue
+            own = members[0].kernel_shapes
+            times = {}
+            for pair in pairs:
+                for p in members:
+                    p.kernel_shapes = pair
+                sub = _native.Batch([p._plan for p in members])
+                try:
+                    sub.steps(torch, warmup, self._device)
+                    stream = torch.cuda.current_stream(self._device)
+                    ev0.record(stream)
+                    sub.steps(torch, n_steps, self._device)
+                    ev1.record(stream)
+                    ev1.synchronize()
+                finally:
+                    sub.close()
+                times[pair] = 1e3 * ev0.elapsed_time(ev1) / n_steps
+            best = min(times, key=times.get)
+            if own in times and times[own] <= (1.0 + margin) * times[best]:
+                best = own
+            for p in members:
+                p.kernel_shapes = best
+            out[key] = times
+        for p, s in zip(self.propagators, saved):
+            p.psik = s
+        return out
 
     def grid_points(self):
         """Total grid points of the batch (sum of Nx*Ny)."""

@@ -37,7 +37,9 @@ def test_shape_counts(native_lib):
     assert lib.sgpe_shape_count(64, 0, 1024) == 2
     assert lib.sgpe_shape_count(64, 1, 1024) == 1
     assert lib.sgpe_shape_count(64, 0, 2048) == 1
-    assert lib.sgpe_shape_count(64, 0, 768) == 1
+    assert lib.sgpe_shape_count(64, 0, 768) == 2
+    assert lib.sgpe_shape_count(64, 1, 192) == 2
+    assert lib.sgpe_shape_count(128, 0, 768) == 1
     assert lib.sgpe_shape_count(128, 0, 256) == 2
     assert lib.sgpe_shape_count(128, 1, 2048) == 1
     assert lib.sgpe_shape_count(64, 0, 48) == 0
@@ -152,6 +154,26 @@ def test_raman_512_complex64_every_shape(tp, tmp_path):
     for shapes in _pairs(64, 512, 512):
         prop = tp.TensorPropagator(ps, 1e-3, n, 'cuda', time='real', dtype=64, kernel_shapes=shapes)
         prop.full_steps(n)
+        assert rel_l2(_psik(prop), ref) <= 1e-5, shapes
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('n', [192, 384, 768])
+def test_radix3_sides_every_shape(tp, tmp_path, n):
+    """Sides 3 * 2^k: both radix plans (12 or 24 points per thread) against
+    the oracle, complex64 real time."""
+    from spinor_gpe import workloads
+    from spinor_gpe.pspinor import pspinor as spin
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    ps = workloads.raman_quench_1024(spin.PSpinor, ttools.fft_2d, str(tmp_path / 'q') + '/',
+                                     n=n, delta=0.5)
+    steps = 3
+    ref = _oracle(ps, 1e-3, 'real', steps)
+    pairs = _pairs(64, n, n)
+    assert len(pairs) == 4
+    for shapes in pairs:
+        prop = tp.TensorPropagator(ps, 1e-3, steps, 'cuda', time='real', dtype=64, kernel_shapes=shapes)
+        prop.full_steps(steps)
         assert rel_l2(_psik(prop), ref) <= 1e-5, shapes
 
 
@@ -302,3 +324,34 @@ def test_fft_every_shape_matches_numpy(tp, bits):
             assert rel_l2([o.cpu().numpy() for o in out], ref_r) <= tol, shapes
     finally:
         plan.close()
+
+
+@pytest.mark.gpu
+def test_batch_autotune_keeps_states_and_matches_solves_alone(tp, tmp_path):
+    """PropagatorBatch.autotune picks shapes per grid class, restores every
+    state, and the tuned batch equals its solves stepped alone in the same
+    shapes, bit for bit."""
+    from spinor_gpe import workloads
+    from spinor_gpe.batch import PropagatorBatch
+    from spinor_gpe.pspinor import pspinor as spin
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    spins = workloads.batched_uneven(spin.PSpinor, ttools.fft_2d, str(tmp_path) + '/t/',
+                                     n_solves=5, sizes=(128, 192), seed=31)
+    props = [tp.TensorPropagator(s, 0.02, 20, 'cuda', time='imag', dtype=64) for s in spins]
+    before = [_psik(p) for p in props]
+    batch = PropagatorBatch(props)
+    tuned = batch.autotune(n_steps=8, warmup=9)
+    assert tuned
+    for p, b in zip(props, before):
+        assert np.array_equal(_psik(p), b)
+    for (bits, ny, nx), times in tuned.items():
+        assert sorted(times) == sorted(_pairs(bits, ny, nx))
+        shapes = {p.kernel_shapes for p in props if p._shape == (ny, nx)}
+        assert len(shapes) == 1 and shapes.pop() in times
+    batch.full_steps(13)
+    alone = [tp.TensorPropagator(s, 0.02, 20, 'cuda', time='imag', dtype=64,
+                                 kernel_shapes=p.kernel_shapes) for s, p in zip(spins, props)]
+    for a, p in zip(alone, props):
+        a.full_steps(13)
+        np.testing.assert_array_equal(_psik(a), _psik(p))
+    batch.close()

@@ -212,7 +212,7 @@ namespace {
 template <class W> W twiddle_entry(double re, double im);
 template <> inline float2 twiddle_entry<float2>(double re, double im) { return make_float2(float(re), float(im)); }
 template <> inline double2 twiddle_entry<double2>(double re, double im) { return make_double2(re, im); }
-#if SGPE_TW_COMP
+#if SGPE_TW_COMP || SGPE_F64_DF
 template <> inline float4 twiddle_entry<float4>(double re, double im) {
   const float hr = float(re), hi = float(im);
   return make_float4(hr, hi, float(re - double(hr)), float(im - double(hi)));

@@ -42,6 +42,21 @@
 #define SGPE_TW_FACTOR 0
 #endif
 
+// Complex128 transforms in double-float arithmetic: the state, the
+// point-wise operators and the reductions stay FP64, while the butterflies
+// of every transform run on FP32 pairs (hi + lo, ~48 significant bits) with
+// head + tail twiddle tables.  (1) on, (0) FP64 butterflies.  Off: measured
+// on GB300 (complex128 imaginary-time steps, default shapes) 64^2 111 ->
+// 117 us, 128^2 125 -> 127 us, 256^2 158 -> 147 us, 512^2 599 -> 458 us,
+// while the transforms' ~48-bit accuracy breaks the original's FFT
+// invariant on an all-ones 256x128 grid (atom number to 10 eps per point:
+// 8.7e-11 against a bound of 7.3e-11).
+#ifndef SGPE_F64_DF
+#define SGPE_F64_DF 0
+#endif
+
+#include <type_traits>
+
 #include "sgpe_tc.cuh"
 
 namespace sgpe {
@@ -51,15 +66,72 @@ template <> struct CxT<float> { using type = float2; };
 template <> struct CxT<double> { using type = double2; };
 template <typename R> using Cx = typename CxT<R>::type;
 
-// Element type of the twiddle tables (see SGPE_TW_COMP).
+// Double-float scalar: the value hi + lo with |lo| <= ulp(hi)/2.  Sums use
+// Knuth's TwoSum on the heads (the tails added without a second TwoSum, an
+// error of order 2^-47 of the operands' magnitude), products Dekker's
+// exact-product identity through an FMA, each renormalised with
+// FastTwoSum.  FP32 only.
+struct DF {
+  float hi, lo;
+  DF() = default;
+  __host__ __device__ constexpr DF(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ constexpr explicit DF(double d) : hi(float(d)), lo(float(d - double(float(d)))) {}
+};
+// (the _rn intrinsics keep the compiler from contracting these sequences
+// into FMAs, which would break the error-free transformations)
+__device__ __forceinline__ DF df_fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return DF(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ DF operator+(DF a, DF b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  return df_fast_two_sum(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ DF operator-(DF a) { return DF(-a.hi, -a.lo); }
+__device__ __forceinline__ DF operator-(DF a, DF b) { return a + (-b); }
+__device__ __forceinline__ DF operator*(DF a, DF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return df_fast_two_sum(p, e);
+}
+struct DFC {
+  DF x, y;
+};
+__device__ __forceinline__ DF to_df(double d) {
+  const float h = __double2float_rn(d);
+  return DF(h, __double2float_rn(d - double(h)));
+}
+__device__ __forceinline__ double from_df(DF a) { return double(a.hi) + double(a.lo); }
+__device__ __forceinline__ DFC to_dfc(double2 z) { return DFC{to_df(z.x), to_df(z.y)}; }
+__device__ __forceinline__ double2 from_dfc(DFC z) { return make_double2(from_df(z.x), from_df(z.y)); }
+// conversion between a storage complex type CS and a compute type C
+template <class C, class CS> __device__ __forceinline__ C to_compute(CS z) {
+  if constexpr (std::is_same<C, CS>::value) return z;
+  else return to_dfc(z);
+}
+template <class CS, class C> __device__ __forceinline__ CS to_storage(C z) {
+  if constexpr (std::is_same<C, CS>::value) return z;
+  else return from_dfc(z);
+}
+
+// Element type of the twiddle tables (see SGPE_TW_COMP, SGPE_F64_DF).
 template <typename R> struct TwT { using type = Cx<R>; };
 #if SGPE_TW_COMP
 template <> struct TwT<float> { using type = float4; };
 #endif
+#if SGPE_F64_DF
+template <> struct TwT<double> { using type = float4; };
+#endif
+template <> struct TwT<DF> { using type = float4; };
 template <typename R> using TwE = typename TwT<R>::type;
 
 __device__ __forceinline__ float fmadd(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double fmadd(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ DF fmadd(DF a, DF b, DF c) { return a * b + c; }
 
 template <class C> __device__ __forceinline__ C cmake(decltype(C::x) a, decltype(C::x) b) {
   C r; r.x = a; r.y = b; return r;
@@ -87,6 +159,11 @@ template <int DIR> __device__ __forceinline__ float2 tw_mul(float2 a, float4 w) 
   }
   const float tr = fmadd(a.x, w.z, a.y * w.w), ti = fmadd(a.y, w.z, -a.x * w.w);
   return make_float2(fmadd(a.x, w.x, fmadd(a.y, w.y, tr)), fmadd(a.y, w.x, fmadd(-a.x, w.y, ti)));
+}
+// double-float values times a head + tail table entry (hi.x, hi.y, lo.x, lo.y)
+template <int DIR> __device__ __forceinline__ DFC tw_mul(DFC a, float4 w) {
+  const DFC wc{DF(w.x, w.z), DF(w.y, w.w)};
+  return DIR < 0 ? cmul(a, wc) : cmulc(a, wc);
 }
 template <class C> __device__ __forceinline__ decltype(C::x) cabs2(C a) { return fmadd(a.x, a.x, a.y * a.y); }
 // a * (DIR * i): DIR = -1 gives a * (-i), DIR = +1 gives a * i
@@ -448,6 +525,11 @@ template <class C, int E, bool WARP = false, bool TC = false> struct LineSmem {
       else __syncthreads();
     }
   }
+  // the same lines viewed as another complex type of the same size
+  template <class C2> __device__ __forceinline__ LineSmem<C2, E, WARP, TC> retype() const {
+    static_assert(sizeof(C2) == sizeof(C), "retyped lines must keep the element size");
+    return LineSmem<C2, E, WARP, TC>{reinterpret_cast<C2*>(base), line_stride, tc, bar, bar_threads};
+  }
 };
 
 // Compile-time address folding for the exchanges.  A stage reads element
@@ -483,8 +565,10 @@ template <int N, int E, int R, int NS> __host__ __device__ constexpr bool stores
 // result to shared memory instead of registers.  In both cases a thread
 // touches exactly the positions j + m*T it holds in the register layout, so
 // no barrier is needed between a thread's own point-wise pass over those
-// positions and the adjacent transform.
-template <int N, int E, int DIR, int L, int NS, bool FROM_SMEM, bool TO_SMEM, class C, class SM>
+// positions and the adjacent transform.  Those natural-order lines hold the
+// storage type CS (converted from / to the compute type C at that boundary);
+// the exchanges between stages hold C.
+template <int N, int E, int DIR, int L, int NS, bool FROM_SMEM, bool TO_SMEM, class C, class SM, class CS = C>
 __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, const C* __restrict__ tw) {
   constexpr int T = N / E;
   constexpr int R = stage_radix(N, E, NS);
@@ -503,6 +587,9 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
       for (int r = 0; r < R; ++r) {
         if constexpr (kFirst && !FROM_SMEM) {
           a[l][q][r] = v[l][q + r * Q];
+        } else if constexpr (kFirst && !std::is_same<C, CS>::value) {
+          const CS* line = reinterpret_cast<const CS*>(sm.line(l));
+          a[l][q][r] = to_compute<C>(line[SM::pad(unsigned(j + q * T + r * (N / R)))]);
         } else if constexpr (kLdFold) {
           const int c = q * T + r * (N / R);
           a[l][q][r] = sm.line(l)[pj + unsigned(c + c / E)];
@@ -565,7 +652,11 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
       for (int q = 0; q < Q; ++q) {
         const int vt = j + q * T;
         const int base = (vt / NS) * NS * R + (vt % NS);
-        if constexpr (kStFold) {
+        if constexpr (kLast && !std::is_same<C, CS>::value) {
+          CS* line = reinterpret_cast<CS*>(sm.line(l));
+#pragma unroll
+          for (int r = 0; r < R; ++r) line[SM::pad(unsigned(base + r * NS))] = to_storage<CS>(a[l][q][r]);
+        } else if constexpr (kStFold) {
           C* sp = sm.line(l) + SM::pad(unsigned(base));
 #pragma unroll
           for (int r = 0; r < R; ++r) sp[r * NS + (r * NS) / E] = a[l][q][r];
@@ -576,7 +667,7 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
       }
     if constexpr (!kLast) {
       sm.sync();
-      fft_stage<N, E, DIR, L, NS * R, FROM_SMEM, TO_SMEM>(v, j, sm, tw);
+      fft_stage<N, E, DIR, L, NS * R, FROM_SMEM, TO_SMEM, C, SM, CS>(v, j, sm, tw);
     }
   }
 }
@@ -589,10 +680,35 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
 // have synchronised after other threads wrote it, unless each thread wrote
 // only its own positions); with TO_SMEM the output is left there in natural
 // order and `v` is not written.
+// With SGPE_F64_DF, complex128 lines are transformed in double-float
+// arithmetic: the points are split into FP32 heads and tails on entry
+// (registers, or the natural-order line in shared memory), the exchanges
+// carry double-float values, and the result is joined back to FP64 on exit;
+// the twiddle tables are then head + tail entries.
 template <int N, int E, int DIR, int L, bool FROM_SMEM = false, bool TO_SMEM = false, class C, class SM>
 __device__ __forceinline__ void fft_lines(C (&v)[L][E], int j, const SM& sm, const C* __restrict__ tw) {
   static_assert(N % E == 0, "N must be a multiple of E");
-  fft_stage<N, E, DIR, L, 1, FROM_SMEM, TO_SMEM>(v, j, sm, tw);
+  if constexpr (SGPE_F64_DF && std::is_same<C, double2>::value) {
+    static_assert(!SGPE_TW_FACTOR, "factorised twiddles read plain complex tables");
+    DFC w[L][E];
+    if constexpr (!FROM_SMEM) {
+#pragma unroll
+      for (int l = 0; l < L; ++l)
+#pragma unroll
+        for (int m = 0; m < E; ++m) w[l][m] = to_dfc(v[l][m]);
+    }
+    const auto smd = sm.template retype<DFC>();
+    fft_stage<N, E, DIR, L, 1, FROM_SMEM, TO_SMEM, DFC, decltype(smd), double2>(w, j, smd,
+                                                                              reinterpret_cast<const DFC*>(tw));
+    if constexpr (!TO_SMEM) {
+#pragma unroll
+      for (int l = 0; l < L; ++l)
+#pragma unroll
+        for (int m = 0; m < E; ++m) v[l][m] = from_dfc(w[l][m]);
+    }
+  } else {
+    fft_stage<N, E, DIR, L, 1, FROM_SMEM, TO_SMEM>(v, j, sm, tw);
+  }
 }
 
 }  // namespace sgpe

@@ -254,13 +254,14 @@ template <typename R> void* upload_twiddles(int n, int e, cudaError_t* err) {
 // the pace.  Step times (us), shape (0,0) -> default:
 //   complex64   32^2 24 -> 15, 64^2 26 -> 15, 128^2 27 -> 16,
 //              256^2 29 -> 21, 512^2 69 -> 40;
-//   complex128  64^2 234 -> 131, 128^2 258 -> 145, 256^2 325 -> 182.
+//   complex128  64^2 234 -> 85, 128^2 258 -> 96, 256^2 325 -> 178 (real
+//               time; imaginary time ranks alike).
 int default_shape(int bits, int axis, int n) {
   struct Entry {
     int n, row, col;
   };
   static const Entry f32[] = {{32, 2, 1}, {64, 2, 2}, {128, 2, 1}, {256, 2, 0}, {512, 1, 0}};
-  static const Entry f64[] = {{32, 1, 1}, {64, 1, 1}, {128, 1, 1}, {256, 1, 1}, {512, 0, 0}};
+  static const Entry f64[] = {{32, 2, 1}, {64, 2, 1}, {128, 2, 1}, {256, 2, 0}, {512, 0, 0}};
   for (const Entry& x : (bits == 64 ? f32 : f64))
     if (x.n == n) return axis == 0 ? x.row : x.col;
   return 0;

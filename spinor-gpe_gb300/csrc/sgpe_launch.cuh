@@ -106,16 +106,21 @@ template <> struct ShapeTune<float> {
   static constexpr int col_shapes(int n) { return n % 3 == 0 ? 2 : (is_pow2(n) && n <= 512) ? 3 : 1; }
   static constexpr int row_e(int n, int s) { return n % 3 == 0 ? r3_alt(n) : n == 1024 ? 32 : s == 1 ? 8 : 4; }
   static constexpr int row_minb(int n, int) { return n == 1024 ? 4 : 0; }  // 0: the shape-0 rule
+  static constexpr int row_threads(int, int) { return Tune<float>::ROW_THREADS; }
   static constexpr int col_e(int n, int) { return n % 3 == 0 ? r3_alt(n) : 8; }
   static constexpr int cols(int n, int s) { return (n % 3 != 0 && s == 2) ? 4 : Tune<float>::COLS; }
 };
+// complex128: 4 points per thread up to 512; shape 2 also halves the lines
+// per block (128-thread row blocks, 2-column tiles of 32-byte row segments),
+// so that grids of up to 256^2 give every SM a block of FP64 butterflies
 template <> struct ShapeTune<double> {
-  static constexpr int row_shapes(int n) { return (is_pow2(n) && n <= 512) ? 2 : 1; }
-  static constexpr int col_shapes(int n) { return (is_pow2(n) && n <= 512) ? 2 : 1; }
+  static constexpr int row_shapes(int n) { return (is_pow2(n) && n <= 512) ? 3 : 1; }
+  static constexpr int col_shapes(int n) { return (is_pow2(n) && n <= 512) ? 3 : 1; }
   static constexpr int row_e(int, int) { return 4; }
   static constexpr int row_minb(int, int) { return 0; }
+  static constexpr int row_threads(int, int s) { return s == 2 ? 128 : Tune<double>::ROW_THREADS; }
   static constexpr int col_e(int, int) { return 4; }
-  static constexpr int cols(int, int) { return Tune<double>::COLS; }
+  static constexpr int cols(int, int s) { return s == 2 ? 2 : Tune<double>::COLS; }
 };
 template <typename R> constexpr int row_shape_count(int n) { return ShapeTune<R>::row_shapes(n); }
 template <typename R> constexpr int col_shape_count(int n) { return ShapeTune<R>::col_shapes(n); }
@@ -126,7 +131,8 @@ template <typename R, int N, int S = 0> struct RowCfg {
                                   : cmin(N, ShapeTune<R>::row_e(N, S));
   static constexpr int T = N / E;
   // threads: 2 components x T per row; at least one warp, at most 16 rows
-  static constexpr int ROWS = cmax(cmax(cmin(Tune<R>::ROW_THREADS / (2 * T), 16), 1), 32 / (2 * T));
+  static constexpr int RT = S == 0 ? Tune<R>::ROW_THREADS : ShapeTune<R>::row_threads(N, S);
+  static constexpr int ROWS = cmax(cmax(cmin(RT / (2 * T), 16), 1), 32 / (2 * T));
   static constexpr int THREADS = 2 * T * ROWS;
   static constexpr size_t SMEM = 2ull * ROWS * (N + N / E) * sizeof(Cx<R>);
   static constexpr int MINB_RULE =

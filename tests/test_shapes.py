@@ -40,7 +40,7 @@ def test_shape_counts(native_lib):
     assert lib.sgpe_shape_count(64, 0, 768) == 2
     assert lib.sgpe_shape_count(64, 1, 192) == 2
     assert lib.sgpe_shape_count(128, 0, 768) == 1
-    assert lib.sgpe_shape_count(128, 0, 256) == 2
+    assert lib.sgpe_shape_count(128, 0, 256) == 3
     assert lib.sgpe_shape_count(128, 1, 2048) == 1
     assert lib.sgpe_shape_count(64, 0, 48) == 0
     assert lib.sgpe_shape_count(32, 0, 256) == 0

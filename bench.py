@@ -292,18 +292,28 @@ def run_native(args, world, rank, local):
     k = args.steps
     barrier(world)
     torch.cuda.synchronize()
+    # events also split the region into 10 windows (median window reported
+    # beside the whole-region value)
+    n_win = 10 if k >= 10 else 1
+    bounds = [round(w * k / n_win) for w in range(n_win + 1)]
     with ClockSampler(local) as clk:
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        ev0.record(stream)
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(n_win + 1)]
+        evs[0].record(stream)
+        w = 1
         for i in range(k):
             props[i % n_rep].full_steps(1)
-        ev1.record(stream)
+            if i + 1 == bounds[w]:
+                evs[w].record(stream)
+                w += 1
         torch.cuda.synchronize()
     barrier(world)
+    ev0, ev1 = evs[0], evs[-1]
     t_dev = ev0.elapsed_time(ev1) / 1e3
     t_max = max_over_ranks(t_dev, world)
     value = world * k / t_max
+    win_rates = [(bounds[w + 1] - bounds[w]) / (evs[w].elapsed_time(evs[w + 1]) / 1e3)
+                 for w in range(n_win)]
+    median_window = world * statistics.median(win_rates)
 
     # ---- per-pass roofline (same workload, events around every pass)
     col_ms, row_ms = props[0]._plan.time_passes(torch, 50, props[0]._device)
@@ -369,6 +379,8 @@ def run_native(args, world, rank, local):
                          f'{state_bytes >> 20} MiB stepped round-robin',
                    'parallelism': f'replicas x{world}'},
         'grid_point_steps_per_s': value * n * n,
+        'median_window': {'value': median_window, 'unit': UNIT, 'windows': n_win,
+                          'what': 'median over equal windows of the timed steps, CUDA events'},
         'e2e': {'value': world * k / t_e2e, 'unit': UNIT,
                 'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h,
                 'path': 'TensorPropagator.psik= (H2D, pinned) / full_steps(1) '
@@ -623,6 +635,9 @@ def run_reference(args, world, rank, local):
             'value': torch_cuda_reference_rate(inp), 'unit': UNIT,
             'what': 'original algorithm on torch CUDA (torch.fft + ATen, with '
                     'its per-sub-step host synchronisations), complex64'}
+        line['torch_cuda_same_gpu_c128'] = {
+            'value': torch_cuda_reference_rate(inp, steps=10, dtype=128), 'unit': UNIT,
+            'what': 'the same in complex128 (the original\'s default precision)'}
     print(json.dumps(line))
 
 

@@ -15,6 +15,10 @@ import.
 Shapes change the rounding of the transforms (every shape meets the parity
 tolerances), so a run is reproducible bit for bit only with the same
 shapes; the wisdom file records them.
+
+``python -m spinor_gpe.tuning --sides 64 256 512 --dtype 64 --out w.json``
+autotunes square grids of those sides on this GPU, prints the step time of
+every pair and saves the choices.
 """
 import json
 import os

@@ -86,12 +86,13 @@ template <typename R> constexpr int pick_e(int n, int e_pow2) {
 // Kernel shapes.  A pass over lines of one length can run in several
 // shapes: launch configurations that differ in points per thread E (and so in
 // the radix plan and the twiddle tables) and in lines per block.  Shape 0 is
-// the configuration chosen by Tune above; shapes 1 and 2, offered for
-// power-of-two sides up to 512, take fewer points per thread, which gives
-// small grids more warps per SM for more transform stages (ShapeTune).  Every shape
-// computes the same transform; the rounding differs with the radix plan.  A
-// plan picks one shape per axis (built-in defaults measured on GB300, or its
-// autotuner).
+// the configuration chosen by Tune above; the others (ShapeTune) take fewer
+// points per thread or fewer lines per block for power-of-two sides up to
+// 512, which gives small grids more warps and blocks per SM for more
+// transform stages, 32 points per thread for complex64 rows of 1024, and the
+// other multiple of 3 for sides 3 * 2^k.  Every shape computes the same
+// transform; the rounding differs with the radix plan.  A plan picks one
+// shape per axis (built-in defaults measured on GB300, or its autotuner).
 constexpr int kMaxShapes = 3;
 constexpr bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 template <typename R> struct ShapeTune;

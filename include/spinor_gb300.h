@@ -243,11 +243,13 @@ int sgpe_set_dft_mode(sgpe_plan* plan, int mode);
 
 /* Kernel shapes.  Each pass (axis 0: the row pass along x, axis 1: the
  * column pass along y) can run in one of several launch configurations for
- * the same side: shape 0 and, for power-of-two sides up to 512, shapes with
- * fewer points per thread (more threads per line, more transform stages),
- * which give small grids more warps per SM.  All shapes compute the same
- * steps; rounding differs with the radix plan (every shape meets the parity
- * tolerances).  A new plan takes built-in defaults measured on GB300.
+ * the same side: shape 0 and, depending on the side and precision, shapes
+ * with fewer points per thread or fewer lines per block (power-of-two sides
+ * up to 512: more warps and blocks for small grids), with 32 points per
+ * thread (complex64 rows of 1024), or with the other radix-3 plan (sides
+ * 3 * 2^k).  All shapes compute the same steps; rounding differs with the
+ * radix plan (every shape meets the parity tolerances).  A new plan takes
+ * built-in defaults measured on GB300.
  * No counterpart in the original (whose transforms are cuFFT's).
  *
  * sgpe_shape_count: number of shapes for (dtype_bits, axis, side n), 0 if n

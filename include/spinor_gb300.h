@@ -290,20 +290,25 @@ int sgpe_autotune(sgpe_plan* plan, int n_steps, int* row_shape, int* col_shape, 
 /* Allocation-free variant of sgpe_fft2, without a plan.  No counterpart in
  * the original package.
  * For callers that must not allocate device memory where they need the
- * transform: code inside an open CUDA stream capture, hosts whose device
- * memory belongs to their own pool allocator, real-time loops that cannot
- * take an allocation's latency or implicit synchronisation, foreign-language
- * hosts holding only raw device pointers.  It calls no cudaMalloc/cudaFree
+ * transform: hosts whose device memory belongs to their own pool allocator
+ * (which has taken the device's free memory and must not be bypassed),
+ * real-time loops that cannot take an allocation's latency or implicit
+ * synchronisation, foreign-language hosts holding only raw device pointers.  It calls no cudaMalloc/cudaFree
  * and no allocating library routine; the caller passes inputs and outputs.
  * Scratch: a file-scope device array of SGPE_FFT2_STATIC_BYTES, enough for
  * grids of up to 65,536 points in complex128 and 131,072 in complex64
  * (e.g. 256x256 and 256x512); larger grids return SGPE_ERR_ARG with a
  * message -- use sgpe_fft2 with a plan for those.
- * Runs on the current CUDA device.  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress) and should be made before
- * any stream capture on that device is started.  All calls share the array:
- * calls that overlap on the GPU (other streams or threads) race -- order
- * them on one stream.  Arguments and results as sgpe_fft2. */
+ * Runs on the current CUDA device, in the runtime API's primary context.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) and should be made before any stream capture on
+ * that device is started.  Under CUDA's default lazy module loading the first
+ * launch of a kernel loads its module, which allocates device memory, and
+ * each (grid size, precision, direction) uses its own kernels: make one
+ * warm-up call per combination before the code that cannot allocate, or set
+ * CUDA_MODULE_LOADING=EAGER.  All calls share the array: calls that overlap
+ * on the GPU (other streams or threads) race -- order them on one stream.
+ * Arguments and results as sgpe_fft2. */
 int sgpe_fft2_static(int ny, int nx, int dtype_bits, const void* in0, const void* in1, void* out0, void* out1,
                      int inverse, double scale, void* stream);
 

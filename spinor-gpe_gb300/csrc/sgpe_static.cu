@@ -2,10 +2,10 @@
 //
 // Who needs it: callers that cannot call cudaMalloc (or anything that
 // allocates device memory) at the point where they want a transform --
-// code running while a CUDA stream capture is open, hosts whose device
-// memory is owned by their own pool allocator and must not be bypassed,
-// real-time loops that cannot afford an allocation's latency or implicit
-// synchronisation, and foreign-language hosts that hold only raw device
+// hosts whose device memory is owned by their own pool allocator, which has
+// taken the device's free memory and must not be bypassed; real-time loops
+// that cannot afford an allocation's latency or its implicit
+// synchronisation; foreign-language hosts that hold only raw device
 // pointers.  sgpe_fft2 needs a plan, and creating a plan allocates; this
 // entry point needs nothing but the caller's input and output buffers.
 //
@@ -15,15 +15,26 @@
 // exits.  Host code cannot use the array's name as a device address (it is a
 // host-side stand-in); the device address is looked up once per device with
 // cudaGetSymbolAddress, with that device current, on the first call made on
-// it.  That first call on a device should therefore come before any stream
-// capture is started on it.
+// it, and kept per device index.  The runtime API's primary context is the
+// one supported: a caller that makes another driver context current, or
+// resets the device, must not rely on the kept address.  That first call on a
+// device should come before any stream capture is started on it.  Under
+// CUDA's default lazy module loading the first launch of each kernel loads
+// its module, which allocates device memory; the transform kernels of each
+// (grid size, precision, direction) are separate kernels, so a caller that
+// cannot allocate later makes one warm-up call per combination it will use
+// (or sets CUDA_MODULE_LOADING=EAGER).
 //
 // All calls share the one array and leave their data in it.  Nothing in it
-// has to start at zero: each call writes its twiddle tables and every
-// element of the intermediate field before reading them.  Calls whose work
-// overlaps on the GPU (different streams, or different host threads) race on
+// has to start at zero: each call writes every element of the intermediate
+// field before reading it, and writes the twiddle tables unless the previous
+// call on that device had the same grid and precision (the tables are then
+// already in place, in stream order).  Calls whose work overlaps on the GPU
+// (different streams without ordering, or different host threads) race on
 // the array; order them on one stream.
+#include <atomic>
 #include <cmath>
+#include <mutex>
 #include <string>
 
 #include "sgpe_launch.cuh"
@@ -38,24 +49,29 @@ namespace {
 static __device__ __align__(256) unsigned char g_fft2_scratch[SGPE_FFT2_STATIC_BYTES];
 
 constexpr int kMaxDevices = 64;
-void* g_scratch_dev[kMaxDevices] = {nullptr};
+std::atomic<void*> g_scratch_dev[kMaxDevices];
+// Per device: the (grid, precision) whose twiddle tables the array holds
+// (0: none or unknown).  g_tw_mutex orders the check-and-rebuild.
+std::atomic<unsigned long long> g_tw_key[kMaxDevices];
+std::mutex g_tw_mutex;
 
 // Device address of the scratch array on the current device (set-up on the
 // first call per device).
-int scratch_address(void** out) {
+int scratch_address(int* dev_out, void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return sgpe_detail::set_error(SGPE_ERR_CUDA, std::string("fft2_static: ") + cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return sgpe_detail::set_error(SGPE_ERR_ARG, "fft2_static: device index too large");
-  if (g_scratch_dev[dev] == nullptr) {
-    void* p = nullptr;
+  void* p = g_scratch_dev[dev].load(std::memory_order_acquire);
+  if (p == nullptr) {
     e = cudaGetSymbolAddress(&p, g_fft2_scratch);
     if (e != cudaSuccess)
       return sgpe_detail::set_error(SGPE_ERR_CUDA, std::string("fft2_static: cudaGetSymbolAddress: ") +
                                                        cudaGetErrorString(e));
-    g_scratch_dev[dev] = p;
+    g_scratch_dev[dev].store(p, std::memory_order_release);  // the same value from any racing thread
   }
-  *out = g_scratch_dev[dev];
+  *dev_out = dev;
+  *out = p;
   return SGPE_OK;
 }
 
@@ -114,17 +130,40 @@ int run(int ny, int nx, const void* i0, const void* i1, void* o0, void* o1, int 
                           " bytes of scratch; the static scratch holds " + std::to_string(SGPE_FFT2_STATIC_BYTES) +
                           " (use sgpe_fft2 with a plan for larger grids)");
   void* base = nullptr;
-  int rc = scratch_address(&base);
+  int dev = 0;
+  int rc = scratch_address(&dev, &base);
   if (rc != SGPE_OK) return rc;
   unsigned char* b = static_cast<unsigned char*>(base);
   C* mid0 = reinterpret_cast<C*>(b);
   C* mid1 = reinterpret_cast<C*>(b + field);
   W* tw_x = reinterpret_cast<W*>(b + 2 * field);
   W* tw_y = reinterpret_cast<W*>(b + 2 * field + round_up(sizeof(W) * (twx > 0 ? twx : 1)));
-  if (twx > 0) twiddle_kernel<R><<<(twx + 255) / 256, 256, 0, s>>>(tw_x, nx, ex, twx);
-  if (twy > 0) twiddle_kernel<R><<<(twy + 255) / 256, 256, 0, s>>>(tw_y, ny, ey, twy);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return sgpe_detail::set_error(SGPE_ERR_CUDA, std::string("fft2_static: ") + cudaGetErrorString(e));
+  cudaError_t e = cudaSuccess;
+  {
+    // twiddle tables of this grid and precision, unless the previous call
+    // on this device left them in place (launch status read from the launch
+    // calls themselves, so an error left pending by the caller's own earlier
+    // work is neither reported here nor cleared)
+    const unsigned long long key =
+        (static_cast<unsigned long long>(ny) << 32) | (static_cast<unsigned long long>(nx) << 8) | sizeof(R);
+    std::lock_guard<std::mutex> lock(g_tw_mutex);
+    if (g_tw_key[dev].load() != key) {
+      g_tw_key[dev].store(0);
+      auto build = [&](W* out, int n, int ep, int total) -> cudaError_t {
+        if (total <= 0) return cudaSuccess;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((total + 255) / 256);
+        cfg.blockDim = dim3(256);
+        cfg.stream = s;
+        return cudaLaunchKernelEx(&cfg, twiddle_kernel<R>, out, n, ep, total);
+      };
+      e = build(tw_x, nx, ex, twx);
+      if (e == cudaSuccess) e = build(tw_y, ny, ey, twy);
+      if (e != cudaSuccess)
+        return sgpe_detail::set_error(SGPE_ERR_CUDA, std::string("fft2_static: ") + cudaGetErrorString(e));
+      g_tw_key[dev].store(key);
+    }
+  }
 
   sgpe::RowArgs<R> r{};
   r.tw = reinterpret_cast<const C*>(tw_x);

@@ -48,42 +48,56 @@ class PropagatorBatch:
         class step}} for the classes that had a choice."""
         lib = _native.load()
         saved = [[t.clone() for t in p.psik] for p in self.propagators]
+        own_shapes = [p.kernel_shapes for p in self.propagators]
         classes = {}
         for p in self.propagators:
             classes.setdefault((p._bits,) + tuple(p._shape), []).append(p)
         out = {}
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
-        for key, members in classes.items():
-            bits, ny, nx = key
-            pairs = list(itertools.product(range(lib.sgpe_shape_count(bits, 0, nx)),
-                                           range(lib.sgpe_shape_count(bits, 1, ny))))
-            if len(pairs) < 2 or any(p.tensor_core_dft for p in members):
-                continue
-            own = members[0].kernel_shapes
-            times = {}
-            for pair in pairs:
+        chosen = {}
+        try:
+            for key, members in classes.items():
+                bits, ny, nx = key
+                pairs = list(itertools.product(range(lib.sgpe_shape_count(bits, 0, nx)),
+                                               range(lib.sgpe_shape_count(bits, 1, ny))))
+                if len(pairs) < 2 or any(p.tensor_core_dft for p in members):
+                    continue
+                own = members[0].kernel_shapes
+                times = {}
+                for pair in pairs:
+                    try:
+                        for p in members:
+                            p.kernel_shapes = pair
+                    except _native.SgpeError:
+                        # a column tile of this shape does not divide nx
+                        # (the per-plan autotuner skips such pairs too)
+                        continue
+                    sub = _native.Batch([p._plan for p in members])
+                    try:
+                        sub.steps(torch, warmup, self._device)
+                        stream = torch.cuda.current_stream(self._device)
+                        ev0.record(stream)
+                        sub.steps(torch, n_steps, self._device)
+                        ev1.record(stream)
+                        ev1.synchronize()
+                    finally:
+                        sub.close()
+                    times[pair] = 1e3 * ev0.elapsed_time(ev1) / n_steps
+                if not times:
+                    continue
+                best = min(times, key=times.get)
+                if own in times and times[own] <= (1.0 + margin) * times[best]:
+                    best = own
                 for p in members:
-                    p.kernel_shapes = pair
-                sub = _native.Batch([p._plan for p in members])
-                try:
-                    sub.steps(torch, warmup, self._device)
-                    stream = torch.cuda.current_stream(self._device)
-                    ev0.record(stream)
-                    sub.steps(torch, n_steps, self._device)
-                    ev1.record(stream)
-                    ev1.synchronize()
-                finally:
-                    sub.close()
-                times[pair] = 1e3 * ev0.elapsed_time(ev1) / n_steps
-            best = min(times, key=times.get)
-            if own in times and times[own] <= (1.0 + margin) * times[best]:
-                best = own
-            for p in members:
-                p.kernel_shapes = best
-            out[key] = times
-        for p, s in zip(self.propagators, saved):
-            p.psik = s
+                    chosen[id(p)] = best
+                out[key] = times
+        finally:
+            # every solve ends in its chosen (else its own) shapes, with the
+            # state it had before tuning
+            for p, own, s in zip(self.propagators, own_shapes, saved):
+                p.kernel_shapes = chosen.get(id(p), own)
+                p.psik = s
         return out
 
     def grid_points(self):

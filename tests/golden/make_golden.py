@@ -1,10 +1,11 @@
 """Generate the golden fixtures in this folder by running the original
 spinor-gpe package on the CPU.
 
-Run from the repository root, where the original package is checked out at
-``/root/reference`` (read-only) and can be imported::
+Run from the repository root with the path of a checkout of the original
+package (read-only is enough), as the first argument or in the environment
+variable ``SPINOR_GPE_REFERENCE``::
 
-    python tests/golden/make_golden.py [/path/to/spinor-gpe]
+    python tests/golden/make_golden.py /path/to/spinor-gpe
 
 matplotlib and scikit-image are imported at module level by the original
 package (``spinor_gpe/pspinor/tensor_tools.py:7``,
@@ -36,7 +37,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get('SPINOR_GPE_REFERENCE')
+if not REF:
+    sys.exit('usage: python tests/golden/make_golden.py /path/to/spinor-gpe '
+             '(or set SPINOR_GPE_REFERENCE)')
 
 
 def _install_stubs():

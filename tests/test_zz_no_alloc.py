@@ -1,13 +1,14 @@
 """The allocation-free transform entry point, sgpe_fft2_static.
 
 It serves callers that cannot allocate device memory where they need a
-transform (inside an open stream capture, under a host-owned pool
-allocator, in latency-critical loops, from foreign-language hosts holding raw
-pointers): it uses a static device scratch array instead of a plan.  Here it
-is called through the C ABI and compared with the plan-based sgpe_fft2 on two
-consecutive calls with different data, forward and inverse, in both
-precisions, at the tolerances of the other transform tests.  The file is
-named so that pytest collects it last.
+transform (a host-owned pool allocator that holds the device's free memory,
+latency-critical loops, foreign-language hosts holding raw pointers): it
+uses a static device scratch array instead of a plan.  Here it is called
+through the C ABI and compared with the plan-based sgpe_fft2 and with
+NumPy's centred transform on two consecutive calls with different data,
+forward and inverse, in both precisions, at the tolerances of the other
+transform tests; after a warm-up call, repeat calls leave the device's free
+memory unchanged.  The file is named so that pytest collects it last.
 """
 import ctypes
 
@@ -19,6 +20,7 @@ from conftest import rel_l2
 
 pytestmark = pytest.mark.gpu
 
+# the transform tests' tolerances, against the plan path and against NumPy
 TOL = {torch.complex64: 2e-6, torch.complex128: 1e-14}
 
 
@@ -62,7 +64,33 @@ def test_static_transform_matches_plan_transform(native, dtype, shape):
             g = np.array([t.cpu().numpy() for t in got])
             assert np.isfinite(g).all(), (call, inverse)
             assert rel_l2(g, r) <= TOL[dtype], (call, inverse)
+            # directly against NumPy: forward = scale * fftshift(fft2(x)),
+            # inverse = scale * (unnormalised inverse of ifftshift(x))
+            x = np.array([t.cpu().numpy() for t in inp]).astype(np.complex128)
+            if inverse:
+                want = np.fft.ifft2(np.fft.ifftshift(x, axes=(1, 2)), axes=(1, 2)) * (nx * ny) * scale
+            else:
+                want = np.fft.fftshift(np.fft.fft2(x, axes=(1, 2)), axes=(1, 2)) * scale
+            assert rel_l2(g, want) <= TOL[dtype], (call, inverse)
     plan.close()
+
+
+def test_static_transform_allocates_nothing_on_repeat_calls(native):
+    shape = (128, 256)
+    inp = [torch.randn(shape, dtype=torch.complex64, device='cuda') for _ in range(2)]
+    out = [torch.empty_like(inp[0]) for _ in range(2)]
+    for inverse in (0, 1):                     # warm-up: loads the kernels' modules
+        assert _static(native, inp, out, inverse, 1.0) == native.SGPE_OK
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    stats0 = torch.cuda.memory_stats().get('allocation.all.allocated', 0)
+    for _ in range(3):
+        for inverse in (0, 1):
+            assert _static(native, inp, out, inverse, 1.0) == native.SGPE_OK
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert torch.cuda.memory_stats().get('allocation.all.allocated', 0) == stats0
 
 
 def test_static_transform_rejects_grids_beyond_its_scratch(native):

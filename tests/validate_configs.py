@@ -16,6 +16,16 @@ solver's steps/s.
 * vortex_2048: 2048^2, complex64 with FP32 DFTs, complex64 with the
   split-BF16 tensor-core DFT16 stages, and complex128; 2000 imaginary steps
   at dt = 0.01, 8 seeded vortices.
+* curve_quench_1024, curve_vortex_2048: the error against the complex128
+  oracle every 500 steps over the whole run (the quench: 3000 imaginary
+  steps, then 10000 real-time steps, each implementation continuing from
+  its own ground state; the vortex start: 2000 imaginary steps), for the
+  solver in each precision, the original's own complex64 arithmetic, and
+  two diagnostic complex128 oracle runs that isolate one FP32 effect each:
+  the state rounded to complex64 after every sub-step (FP32 storage alone),
+  and the operator tables rounded to complex64 (FP32 tables alone).  Besides
+  the relative L2 error, the error after removing the best global phase is
+  recorded.
 """
 import json
 import os
@@ -142,12 +152,171 @@ def vortex_2048(tmp):
                 mine, ref, rate, {'original_complex64_psik_rel_l2': rel_l2(ref64, ref)})
 
 
+# ----------------------------------------------------- error-vs-step curves
+
+class RoundedStateOracle(OraclePropagator):
+    """complex128 oracle whose psik is rounded to complex64 after every
+    sub-step: the effect of FP32 storage of the state alone."""
+
+    def single_step(self, t_step, eng):
+        super().single_step(t_step, eng)
+        self.psik = [p.to(torch.complex64).to(torch.complex128) for p in self.psik]
+
+
+class RoundedTablesOracle(OraclePropagator):
+    """complex128 oracle whose pre-computed operator tables (kinetic,
+    potential, coupling) are rounded to complex64: the effect of FP32 tables
+    alone."""
+
+    def __init__(self, *a, **k):
+        super().__init__(*a, **k)
+
+        def rnd(t):
+            return t.to(torch.complex64).to(torch.complex128)
+        for eng in (self.eng_out, self.eng_in):
+            eng['kin'] = [rnd(e) for e in eng['kin']]
+            eng['pot'] = [rnd(e) for e in eng['pot']]
+            eng['coupl'] = [[rnd(e) for e in row] for row in eng['coupl']]
+
+
+def phase_aligned_rel_l2(a, b):
+    """min over a global phase phi of ||a e^{i phi} - b|| / ||b||."""
+    a = np.asarray(a).ravel()
+    b = np.asarray(b).ravel()
+    ov = np.vdot(a, b)
+    ph = ov / abs(ov) if abs(ov) > 0 else 1.0
+    return float(np.linalg.norm(a * ph - b) / np.linalg.norm(b))
+
+
+class OracleRunner:
+    """Checkpointed run of one oracle class (complex128 unless dtype 64)."""
+
+    def __init__(self, cls=OraclePropagator, dtype=128):
+        self.cls, self.dtype = cls, dtype
+
+    def start(self, ps, dt, time_mode):
+        self.orc = self.cls(inputs(ps), dt, time_mode, self.dtype, device='cuda')
+
+    def steps(self, n):
+        for _ in range(n):
+            self.orc.full_step()
+
+    def psik(self):
+        return self.orc.psik_numpy().astype(np.complex128)
+
+
+class SolverRunner:
+    """Checkpointed run of the drop-in propagator in one precision."""
+
+    def __init__(self, dtype, **kw):
+        self.dtype, self.kw = dtype, kw
+        self.busy = 0.0
+
+    def start(self, ps, dt, time_mode):
+        self.prop = tprop.TensorPropagator(ps, dt, 1, 'cuda', time=time_mode,
+                                           dtype=self.dtype, **self.kw)
+
+    def steps(self, n):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        self.prop.full_steps(n)
+        torch.cuda.synchronize()
+        self.busy += time.perf_counter() - t0
+
+    def psik(self):
+        return np.array([p.cpu().numpy() for p in self.prop.psik]).astype(np.complex128)
+
+
+def error_curve(name, build, phases, runners, every=500):
+    """Run every runner through ``phases`` [(dt, n_steps, time, prepare)],
+    where ``prepare(ps)`` (or None) changes the problem before a phase and
+    each runner continues from its own state; print the error against the
+    first runner (the complex128 oracle) every ``every`` steps."""
+    tmp = tempfile.mkdtemp(prefix='sgpe_curve_')
+    ref_points = None
+    for i, (label, runner) in enumerate(runners):
+        ps = build(tmp + f'/run{i}/')
+        points, step = [], 0
+        for dt, n, time_mode, prepare in phases:
+            if step > 0:
+                ps.psik = list(runner.psik())
+            if prepare is not None:
+                prepare(ps)
+            runner.start(ps, dt, time_mode)
+            done = 0
+            while done < n:
+                k = min(every, n - done)
+                runner.steps(k)
+                done += k
+                step += k
+                points.append((step, time_mode, runner.psik()))
+        if ref_points is None:
+            ref_points = points
+            continue
+        curve = [{'step': st, 'time': tm, 'psik_rel_l2': rel_l2(pk, rp[2]),
+                  'phase_aligned_rel_l2': phase_aligned_rel_l2(pk, rp[2])}
+                 for (st, tm, pk), rp in zip(points, ref_points)]
+        out = {'config': name, 'variant': label, 'curve': curve}
+        if isinstance(runner, SolverRunner):
+            out['solver_steps_per_s'] = step / runner.busy
+        print(json.dumps(out), flush=True)
+        del points
+
+
+def curve_runners(variants):
+    """The complex128 oracle (reference), then the named variants."""
+    table = {
+        'original complex64': lambda: OracleRunner(dtype=64),
+        'oracle complex128, state rounded to complex64 each sub-step':
+            lambda: OracleRunner(RoundedStateOracle),
+        'oracle complex128, operator tables rounded to complex64':
+            lambda: OracleRunner(RoundedTablesOracle),
+        'solver complex64': lambda: SolverRunner(64),
+        'solver complex128': lambda: SolverRunner(128),
+    }
+    return [('oracle complex128', OracleRunner())] + [(v, table[v]()) for v in variants]
+
+
+CURVE_VARIANTS = ['original complex64',
+                  'oracle complex128, state rounded to complex64 each sub-step',
+                  'oracle complex128, operator tables rounded to complex64',
+                  'solver complex64', 'solver complex128']
+
+
+def curve_quench_1024(tmp, variants=None):
+    def build(path):
+        return workloads.raman_quench_1024(spin.PSpinor, ttools.fft_2d, path)
+    error_curve('raman_quench_1024 (3000 imag + 10000 real steps)', build,
+                [(0.01, 3000, 'imag', None),
+                 (1e-3, 10000, 'real', lambda ps: ps.detuning_uniform(0.5))],
+                curve_runners(variants or CURVE_VARIANTS))
+
+
+def curve_vortex_2048(tmp, variants=None):
+    def build(path):
+        return workloads.vortex_2048(spin.PSpinor, ttools.fft_2d, path)
+    error_curve('vortex_2048 (2000 imag steps)', build,
+                [(0.01, 2000, 'imag', None)], curve_runners(variants or CURVE_VARIANTS))
+
+
 CONFIGS = {'ground_state_256': ground_state_256,
+           'curve_quench_1024': curve_quench_1024,
+           'curve_vortex_2048': curve_vortex_2048,
            'raman_quench_1024': raman_quench_1024,
            'vortex_2048': vortex_2048}
 
 if __name__ == '__main__':
-    names = sys.argv[1:] or list(CONFIGS)
+    # python tests/validate_configs.py [config ...] [--variants "name" ...]
+    argv = sys.argv[1:]
+    variants = None
+    if '--variants' in argv:
+        k = argv.index('--variants')
+        variants = argv[k + 1:]
+        argv = argv[:k]
+    names = argv or list(CONFIGS)
     tmp = tempfile.mkdtemp(prefix='sgpe_validate_')
     for n in names:
-        CONFIGS[n](tmp)
+        if n.startswith('curve_'):
+            CONFIGS[n](tmp, variants)
+        else:
+            CONFIGS[n](tmp)

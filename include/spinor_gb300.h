@@ -75,9 +75,18 @@ int sgpe_version(void);
 /* Message of the last failing call on this thread ("" if none). */
 const char* sgpe_last_error(void);
 
+/* dtype_bits of the double-float precision: the state, the operator tables
+ * and every transform in pairs of FP32 values (head + tail, about 48
+ * significant bits, 16 bytes per complex value), on the FP32 pipes; psik is
+ * loaded and stored as complex128 and the energy, analysis and sgpe_fft2 of
+ * such a plan take complex128 buffers.  Kernel shape 0 only; not grouped in
+ * batches; no tensor-core DFT. */
+#define SGPE_DTYPE_DF 48
+
 /* Create a plan for an (ny, nx) grid.  Sizes on each axis: powers of two
- * 32..4096, or 192, 384, 768 (3 * 2^k, with a radix-3 stage).  dtype_bits: 64 (complex64) or 128 (complex128).  Allocates the
- * device state on `device`.  Synchronous.
+ * 32..4096, or 192, 384, 768 (3 * 2^k, with a radix-3 stage).  dtype_bits:
+ * 64 (complex64), 128 (complex128) or SGPE_DTYPE_DF (double-float).
+ * Allocates the device state on `device`.  Synchronous.
  * Replaces: TensorPropagator.__init__ tensor uploads
  * (spinor_gpe/pspinor/tensor_propagator.py:111-122). */
 int sgpe_plan_create(sgpe_plan** plan, int ny, int nx, int dtype_bits, int device);

@@ -14,6 +14,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include <cuda.h>
@@ -143,6 +144,10 @@ struct sgpe_plan {
   uint32_t* tcb = nullptr;   // their B fragments (device)
   void* tw_x = nullptr;
   void* tw_y = nullptr;
+  // complex128 twiddle tables of a double-float plan, for its complex128
+  // transforms (sgpe_fft2, the energy functional); made on first use
+  void* tw64_x = nullptr;
+  void* tw64_y = nullptr;
   SubOps sub[2];
   PairOps pair[2][2];        // [prev][next]
   EnergyFields efield[2];
@@ -212,12 +217,24 @@ namespace {
 template <class W> W twiddle_entry(double re, double im);
 template <> inline float2 twiddle_entry<float2>(double re, double im) { return make_float2(float(re), float(im)); }
 template <> inline double2 twiddle_entry<double2>(double re, double im) { return make_double2(re, im); }
-#if SGPE_TW_COMP || SGPE_F64_DF
 template <> inline float4 twiddle_entry<float4>(double re, double im) {
   const float hr = float(re), hi = float(im);
   return make_float4(hr, hi, float(re - double(hr)), float(im - double(hi)));
 }
-#endif
+
+// Calls f(R{}) with R the arithmetic type of a plan's precision: float
+// (complex64), double (complex128) or sgpe::DF (double-float).
+template <class F> auto by_prec(int bits, F&& f) {
+  if (bits == 64) return f(float{});
+  if (bits == 128) return f(double{});
+  return f(sgpe::DF{});
+}
+// ... with R the type of the plan's psik buffers (complex64 or complex128;
+// a double-float plan takes complex128 buffers).
+template <class F> auto by_iface(int bits, F&& f) {
+  if (bits == 64) return f(float{});
+  return f(double{});
+}
 
 // Per-stage twiddle table of an (n, e) transform, in the order the FFT
 // engine reads it (sgpe_fft.cuh: tw_offset): for each stage (ns, r_s),
@@ -262,6 +279,7 @@ int default_shape(int bits, int axis, int n) {
   };
   static const Entry f32[] = {{32, 2, 1}, {64, 2, 2}, {128, 2, 1}, {256, 2, 0}, {512, 1, 0}};
   static const Entry f64[] = {{32, 2, 1}, {64, 2, 1}, {128, 2, 1}, {256, 2, 0}, {512, 0, 0}};
+  if (bits == SGPE_DTYPE_DF) return 0;
   for (const Entry& x : (bits == 64 ? f32 : f64))
     if (x.n == n) return axis == 0 ? x.row : x.col;
   return 0;
@@ -270,6 +288,7 @@ int default_shape(int bits, int axis, int n) {
 int shape_count(int bits, int axis, int n) {
   if (!sgpe::size_supported(n)) return 0;
   if (bits == 64) return axis == 0 ? sgpe::row_shape_count<float>(n) : sgpe::col_shape_count<float>(n);
+  if (bits == SGPE_DTYPE_DF) return axis == 0 ? sgpe::row_shape_count<sgpe::DF>(n) : sgpe::col_shape_count<sgpe::DF>(n);
   return axis == 0 ? sgpe::row_shape_count<double>(n) : sgpe::col_shape_count<double>(n);
 }
 
@@ -304,6 +323,15 @@ int upload_field(sgpe_plan* p, const sgpe_field& f, DevField* out, SubOps* so, c
   if (p->bits == 64) {
     std::vector<float> h(2 * (size_t)f.n);
     for (size_t i = 0; i < h.size(); ++i) h[i] = float(f.data[i]);
+    e = cudaMemcpy(d, h.data(), p->elem * f.n, cudaMemcpyHostToDevice);
+  } else if (p->bits == SGPE_DTYPE_DF) {
+    // (re.hi, re.lo, im.hi, im.lo): the FP64 value as head + tail
+    std::vector<float> h(4 * (size_t)f.n);
+    for (size_t i = 0; i < 2 * (size_t)f.n; ++i) {
+      const float hd = float(f.data[i]);
+      h[2 * i] = hd;
+      h[2 * i + 1] = float(f.data[i] - double(hd));
+    }
     e = cudaMemcpy(d, h.data(), p->elem * f.n, cudaMemcpyHostToDevice);
   } else {
     e = cudaMemcpy(d, f.data, p->elem * f.n, cudaMemcpyHostToDevice);
@@ -616,6 +644,96 @@ template <typename R> int substep(sgpe_plan* p, int sub, double* pops, cudaStrea
   return SGPE_OK;
 }
 
+// Conversion copies of the double-float state (sgpe::DfCopyArgs).
+__global__ void __launch_bounds__(256) df_copy_kernel(const sgpe::DfCopyArgs a) {
+  __shared__ double s_alpha;
+  if (threadIdx.x < 32) {
+    double alpha = 1.0;
+    if (a.part != nullptr) {
+      double s0, s1, sw;
+      sgpe::sum_partials(a.part, a.ntile, threadIdx.x, &s0, &s1, &sw);
+      alpha = sqrt(a.atom_num / (a.dv * (s0 + s1)));
+      if (threadIdx.x == 0 && a.pops != nullptr && blockIdx.x == 0) {
+        a.pops[0] = a.atom_num * s0 / (s0 + s1);
+        a.pops[1] = a.atom_num * s1 / (s0 + s1);
+      }
+    }
+    if (threadIdx.x == 0) s_alpha = alpha;
+  }
+  __syncthreads();
+  const double alpha = s_alpha;
+  const long long n = (long long)a.nx * a.ny;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const int sx = a.shift ? a.nx / 2 : 0, sy = a.shift ? a.ny / 2 : 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int y = int(i / a.nx), x = int(i - (long long)y * a.nx);
+    const long long src = (long long)((y + sy) % a.ny) * a.nx + (x + sx) % a.nx;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      if (a.to_df) {
+        static_cast<sgpe::DFC*>(a.out[c])[i] = sgpe::to_dfc(static_cast<const double2*>(a.in[c])[src]);
+      } else {
+        const double2 z = sgpe::from_dfc(static_cast<const sgpe::DFC*>(a.in[c])[src]);
+        static_cast<double2*>(a.out[c])[i] = make_double2(z.x * alpha, z.y * alpha);
+      }
+    }
+  }
+}
+
+// Double-float state to complex128 psik: in k-space form a converting copy;
+// in mixed form the column pass into the plan's scratch (centred order),
+// then the conversion with the final renormalisation and populations.
+int store_df(sgpe_plan* p, void* o0, void* o1, double* pops, cudaStream_t s) {
+  using R = sgpe::DF;
+  sgpe::DfCopyArgs d{};
+  d.out[0] = o0;
+  d.out[1] = o1;
+  d.nx = p->nx;
+  d.ny = p->ny;
+  d.to_df = 0;
+  if (p->form == kKspace) {
+    d.in[0] = p->s[0];
+    d.in[1] = p->s[1];
+    d.shift = 1;
+  } else {
+    for (int c = 0; c < 2; ++c) {
+      if (p->scratch[c] == nullptr) {
+        const cudaError_t e = cudaMalloc(&p->scratch[c], p->elem * p->nx * p->ny);
+        if (e != cudaSuccess) return fail(SGPE_ERR_OOM, std::string("store scratch: ") + cudaGetErrorString(e));
+      }
+    }
+    sgpe::ColArgs<R> a{};
+    a.in[0] = cst<R>(p->s[0]);
+    a.in[1] = cst<R>(p->s[1]);
+    a.out[0] = st<R>(p->scratch[0]);
+    a.out[1] = st<R>(p->scratch[1]);
+    a.tw = cst<R>(p->tw_y);
+    a.shape = p->col_shape;
+    a.nx = p->nx;
+    a.fwd = 1;
+    a.inv = 0;
+    a.out_shift = 1;
+    a.nk = 1;
+    a.k1 = kin_op<R>(p->sub[p->prev_sub]);
+    a.scale = R(1);
+    a.part = reinterpret_cast<R*>(p->part);
+    const cudaError_t e = sgpe::launch_col<R>(a, p->ny, s);
+    if (e != cudaSuccess) return cuda_fail(e, "store (column pass)");
+    d.in[0] = p->scratch[0];
+    d.in[1] = p->scratch[1];
+    d.shift = 0;
+    d.part = reinterpret_cast<const R*>(p->part);
+    d.ntile = p->ntile;
+    d.atom_num = p->atom_num;
+    d.dv = p->dv_k;
+    d.pops = pops != nullptr ? pops : p->pending_pops;
+    p->pending_pops = nullptr;
+  }
+  df_copy_kernel<<<8 * 152, 256, 0, s>>>(d);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? SGPE_OK : cuda_fail(e, "store (double-float conversion)");
+}
+
 template <typename R> int store(sgpe_plan* p, void* o0, void* o1, double* pops, cudaStream_t s) {
   if (p->form == kKspace) {
     sgpe::CopyArgs<R> c{};
@@ -663,6 +781,37 @@ template <typename R> int store(sgpe_plan* p, void* o0, void* o1, double* pops, 
   return e == cudaSuccess ? SGPE_OK : cuda_fail(e, "store (scale)");
 }
 
+template <> int store<sgpe::DF>(sgpe_plan* p, void* o0, void* o1, double* pops, cudaStream_t s) {
+  return store_df(p, o0, o1, pops, s);
+}
+
+// Twiddle tables for transforms in the arithmetic of R: the plan's own, or,
+// for the complex128 transforms of a double-float plan, complex128 tables of
+// kernel shape 0 made on first use.
+template <typename R> int transform_tables(sgpe_plan* p, const void** tx, const void** ty) {
+  if (!(std::is_same<R, double>::value && p->bits == SGPE_DTYPE_DF)) {
+    *tx = p->tw_x;
+    *ty = p->tw_y;
+    return SGPE_OK;
+  }
+  if (p->tw64_x == nullptr) {
+    cudaError_t e = cudaSuccess;
+    void* x = upload_twiddles<double>(p->nx, sgpe::row_points_per_thread<double>(p->nx, 0), &e);
+    void* y = e == cudaSuccess ? upload_twiddles<double>(p->ny, sgpe::col_points_per_thread<double>(p->ny, 0), &e)
+                               : nullptr;
+    if (e != cudaSuccess) {
+      if (x) cudaFree(x);
+      if (y) cudaFree(y);
+      return fail(SGPE_ERR_OOM, std::string("complex128 twiddle tables: ") + cudaGetErrorString(e));
+    }
+    p->tw64_x = x;
+    p->tw64_y = y;
+  }
+  *tx = p->tw64_x;
+  *ty = p->tw64_y;
+  return SGPE_OK;
+}
+
 template <typename R> int fft2(sgpe_plan* p, const void* i0, const void* i1, void* o0, void* o1,
                                int inverse, double scale, cudaStream_t s) {
   if (p->scratch[0] == nullptr) {
@@ -671,16 +820,22 @@ template <typename R> int fft2(sgpe_plan* p, const void* i0, const void* i1, voi
       if (e != cudaSuccess) return fail(SGPE_ERR_OOM, std::string("fft2 scratch: ") + cudaGetErrorString(e));
     }
   }
+  const void* twx = nullptr;
+  const void* twy = nullptr;
+  const int trc = transform_tables<R>(p, &twx, &twy);
+  if (trc != SGPE_OK) return trc;
+  // the complex128 transforms of a double-float plan run in shape 0
+  const bool own = (p->bits != SGPE_DTYPE_DF);
   sgpe::RowArgs<R> r{};
-  r.tw = cst<R>(p->tw_x);
+  r.tw = cst<R>(twx);
   r.tc = p->tc;
   r.tcb = p->tcb;
-  r.shape = p->row_shape;
+  r.shape = own ? p->row_shape : 0;
   sgpe::ColArgs<R> c{};
-  c.tw = cst<R>(p->tw_y);
+  c.tw = cst<R>(twy);
   c.tc = p->tc;
   c.tcb = p->tcb;
-  c.shape = p->col_shape;
+  c.shape = own ? p->col_shape : 0;
   c.nx = p->nx;
   c.scale = R(1);
   cudaError_t e;
@@ -785,6 +940,7 @@ int energy_impl(sgpe_plan* p, int slot, const void* k0, const void* k1, double* 
 template <typename R> void update_col_tmaps(sgpe_plan* p) {
   p->tmaps_valid = false;
   if (!SGPE_COL_TMA) return;  // the kernels are built without the TMA tiles
+  if (p->bits == SGPE_DTYPE_DF) return;  // plain loads for double-float tiles
   const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   const int cols = sgpe::col_tile_width<R>(p->ny, p->col_shape);
   if (enc == nullptr || cols == 0) return;
@@ -895,7 +1051,7 @@ template <typename R> int apply_shapes(sgpe_plan* p, int rs, int cs) {
 }
 
 int apply_shapes_any(sgpe_plan* p, int rs, int cs) {
-  return p->bits == 64 ? apply_shapes<float>(p, rs, cs) : apply_shapes<double>(p, rs, cs);
+  return by_prec(p->bits, [&](auto t) { return apply_shapes<decltype(t)>(p, rs, cs); });
 }
 
 template <typename R> int full_steps_impl(sgpe_plan* p, int n_steps, double* pops, cudaStream_t s) {
@@ -936,7 +1092,8 @@ int sgpe_plan_create(sgpe_plan** out, int ny, int nx, int dtype_bits, int device
   if (!sgpe::size_supported(nx) || !sgpe::size_supported(ny))
     return fail(SGPE_ERR_ARG, "grid sizes must be powers of two in [32, 4096] or 192, 384, 768, got ny=" + std::to_string(ny) +
                                   " nx=" + std::to_string(nx));
-  if (dtype_bits != 64 && dtype_bits != 128) return fail(SGPE_ERR_ARG, "dtype_bits must be 64 or 128");
+  if (dtype_bits != 64 && dtype_bits != 128 && dtype_bits != SGPE_DTYPE_DF)
+    return fail(SGPE_ERR_ARG, "dtype_bits must be 64, 128 or SGPE_DTYPE_DF (48)");
   DeviceGuard g(device);
   if (!g.ok) return fail(SGPE_ERR_ARG, "cannot select device " + std::to_string(device));
   sgpe_plan* p = new sgpe_plan();
@@ -944,18 +1101,17 @@ int sgpe_plan_create(sgpe_plan** out, int ny, int nx, int dtype_bits, int device
   p->nx = nx;
   p->bits = dtype_bits;
   p->device = device;
-  p->elem = dtype_bits == 64 ? sizeof(float2) : sizeof(double2);
+  p->elem = dtype_bits == 64 ? sizeof(float2) : dtype_bits == 128 ? sizeof(double2) : sizeof(sgpe::DFC);
   // SGPE_DISABLE_GRAPHS (any value) makes this plan launch every step
   // eagerly; used to check graph replay against eager launches.
   p->graphs_enabled = std::getenv("SGPE_DISABLE_GRAPHS") == nullptr;
   p->row_shape = default_shape(dtype_bits, 0, nx);
   p->col_shape = default_shape(dtype_bits, 1, ny);
-  int cols = dtype_bits == 64 ? sgpe::col_tile_width<float>(ny, p->col_shape)
-                              : sgpe::col_tile_width<double>(ny, p->col_shape);
+  int cols = by_prec(dtype_bits, [&](auto t) { return sgpe::col_tile_width<decltype(t)>(ny, p->col_shape); });
   if (cols == 0 || nx % cols != 0 || (nx / 2) % cols != 0) {
     // the default shape's tile does not divide nx: shape 0
     p->col_shape = 0;
-    cols = dtype_bits == 64 ? sgpe::col_tile_width<float>(ny) : sgpe::col_tile_width<double>(ny);
+    cols = by_prec(dtype_bits, [&](auto t) { return sgpe::col_tile_width<decltype(t)>(ny); });
   }
   if (cols == 0 || nx % cols != 0 || (nx / 2) % cols != 0) {
     delete p;
@@ -970,15 +1126,12 @@ int sgpe_plan_create(sgpe_plan** out, int ny, int nx, int dtype_bits, int device
   if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&p->part), red_bytes);
   if (e == cudaSuccess) e = cudaMemset(p->part, 0, red_bytes);
   if (e == cudaSuccess) {
-    if (dtype_bits == 64) {
-      p->tw_x = upload_twiddles<float>(nx, sgpe::row_points_per_thread<float>(nx, p->row_shape), &e);
-      if (e == cudaSuccess)
-        p->tw_y = upload_twiddles<float>(ny, sgpe::col_points_per_thread<float>(ny, p->col_shape), &e);
-    } else {
-      p->tw_x = upload_twiddles<double>(nx, sgpe::row_points_per_thread<double>(nx, p->row_shape), &e);
-      if (e == cudaSuccess)
-        p->tw_y = upload_twiddles<double>(ny, sgpe::col_points_per_thread<double>(ny, p->col_shape), &e);
-    }
+    by_prec(dtype_bits, [&](auto t) {
+      using R = decltype(t);
+      p->tw_x = upload_twiddles<R>(nx, sgpe::row_points_per_thread<R>(nx, p->row_shape), &e);
+      if (e == cudaSuccess) p->tw_y = upload_twiddles<R>(ny, sgpe::col_points_per_thread<R>(ny, p->col_shape), &e);
+      return 0;
+    });
   }
   if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&p->derr), sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(p->derr, 0, sizeof(int));
@@ -987,7 +1140,7 @@ int sgpe_plan_create(sgpe_plan** out, int ny, int nx, int dtype_bits, int device
     return fail(SGPE_ERR_OOM, std::string("plan allocation: ") + cudaGetErrorString(e));
   }
   if (dtype_bits == 64) update_col_tmaps<float>(p);
-  else update_col_tmaps<double>(p);
+  else if (dtype_bits == 128) update_col_tmaps<double>(p);
   *out = p;
   return SGPE_OK;
 }
@@ -1004,6 +1157,8 @@ int sgpe_plan_destroy(sgpe_plan* p) {
   if (p->part) cudaFree(p->part);
   if (p->tw_x) cudaFree(p->tw_x);
   if (p->tw_y) cudaFree(p->tw_y);
+  if (p->tw64_x) cudaFree(p->tw64_x);
+  if (p->tw64_y) cudaFree(p->tw64_y);
   free_sub(p->sub[0]);
   free_sub(p->sub[1]);
   for (int i = 0; i < 2; ++i)
@@ -1203,7 +1358,19 @@ int sgpe_load_psik(sgpe_plan* p, const void* k0, const void* k1, void* stream) {
   DeviceGuard g(p->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   cudaError_t e;
-  if (p->bits == 64) {
+  if (p->bits == SGPE_DTYPE_DF) {
+    sgpe::DfCopyArgs d{};
+    d.in[0] = k0;
+    d.in[1] = k1;
+    d.out[0] = p->s[0];
+    d.out[1] = p->s[1];
+    d.nx = p->nx;
+    d.ny = p->ny;
+    d.shift = 1;
+    d.to_df = 1;
+    df_copy_kernel<<<8 * 152, 256, 0, s>>>(d);
+    e = cudaGetLastError();
+  } else if (p->bits == 64) {
     sgpe::CopyArgs<float> c{};
     c.in[0] = cst<float>(k0);
     c.in[1] = cst<float>(k1);
@@ -1237,7 +1404,7 @@ int sgpe_store_psik(sgpe_plan* p, void* o0, void* o1, double* pops, void* stream
   if (p->form == kEmpty) return fail(SGPE_ERR_STATE, "no state loaded");
   DeviceGuard g(p->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  return p->bits == 64 ? store<float>(p, o0, o1, pops, s) : store<double>(p, o0, o1, pops, s);
+  return by_prec(p->bits, [&](auto t) { return store<decltype(t)>(p, o0, o1, pops, s); });
 }
 
 int sgpe_single_step(sgpe_plan* p, int sub, void* stream) {
@@ -1247,7 +1414,7 @@ int sgpe_single_step(sgpe_plan* p, int sub, void* stream) {
   if (!ready(p)) return fail(SGPE_ERR_STATE, "physics or sub-step operators not set");
   DeviceGuard g(p->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  return p->bits == 64 ? substep<float>(p, sub, nullptr, s) : substep<double>(p, sub, nullptr, s);
+  return by_prec(p->bits, [&](auto t) { return substep<decltype(t)>(p, sub, nullptr, s); });
 }
 
 int sgpe_full_steps(sgpe_plan* p, int n_steps, double* pops, void* stream) {
@@ -1257,8 +1424,7 @@ int sgpe_full_steps(sgpe_plan* p, int n_steps, double* pops, void* stream) {
   if (!ready(p)) return fail(SGPE_ERR_STATE, "physics or sub-step operators not set");
   DeviceGuard g(p->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const int rc = p->bits == 64 ? full_steps_impl<float>(p, n_steps, pops, s)
-                               : full_steps_impl<double>(p, n_steps, pops, s);
+  const int rc = by_prec(p->bits, [&](auto t) { return full_steps_impl<decltype(t)>(p, n_steps, pops, s); });
   if (rc != SGPE_OK) return rc;
   if (pops != nullptr && n_steps > 0) p->pending_pops = pops + 2 * (n_steps - 1);
   return SGPE_OK;
@@ -1295,7 +1461,7 @@ int sgpe_energy(sgpe_plan* p, int slot, const void* k0, const void* k1, double* 
   if (!p->physics) return fail(SGPE_ERR_STATE, "physics not set");
   DeviceGuard g(p->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  return p->bits == 64 ? energy_impl<float>(p, slot, k0, k1, out, s) : energy_impl<double>(p, slot, k0, k1, out, s);
+  return by_iface(p->bits, [&](auto t) { return energy_impl<decltype(t)>(p, slot, k0, k1, out, s); });
 }
 
 }  // extern "C"
@@ -1340,7 +1506,7 @@ int sgpe_analysis(sgpe_plan* p, const void* psi0, const void* psi1, const void* 
   const void* in[4] = {psi0, psi1, psik0, psik1};
   void* out[6] = {dens0, dens1, densk0, densk1, phase0, phase1};
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  return p->bits == 64 ? analysis_impl<float>(p, in, out, sums_dev, s) : analysis_impl<double>(p, in, out, sums_dev, s);
+  return by_iface(p->bits, [&](auto t) { return analysis_impl<decltype(t)>(p, in, out, sums_dev, s); });
 }
 
 int sgpe_time_passes(sgpe_plan* p, int n_steps, double* col_ms, double* row_ms, void* stream) {
@@ -1352,7 +1518,7 @@ int sgpe_time_passes(sgpe_plan* p, int n_steps, double* col_ms, double* row_ms, 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // reach the steady state (mixed form after an outer sub-step) eagerly
   if (!(p->form == kMixed && p->prev_sub == 0 && p->pending_pops == nullptr)) {
-    const int rc = p->bits == 64 ? eager_step<float>(p, nullptr, s) : eager_step<double>(p, nullptr, s);
+    const int rc = by_prec(p->bits, [&](auto t) { return eager_step<decltype(t)>(p, nullptr, s); });
     if (rc != SGPE_OK) return rc;
   }
   for (int a = 0; a < 2; ++a)
@@ -1379,11 +1545,11 @@ int sgpe_time_passes(sgpe_plan* p, int n_steps, double* col_ms, double* row_ms, 
       const int sub = (i % 3 == 1) ? 1 : 0;
       e = cudaEventRecordWithFlags(ev[4 * i + 0], cs, cudaEventRecordExternal);
       if (e == cudaSuccess)
-        e = p->bits == 64 ? col_pass_step<float>(p, sub, nullptr, cs) : col_pass_step<double>(p, sub, nullptr, cs);
+        e = by_prec(p->bits, [&](auto t) { return col_pass_step<decltype(t)>(p, sub, nullptr, cs); });
       if (e == cudaSuccess) e = cudaEventRecordWithFlags(ev[4 * i + 1], cs, cudaEventRecordExternal);
       if (e == cudaSuccess) e = cudaEventRecordWithFlags(ev[4 * i + 2], cs, cudaEventRecordExternal);
       if (e == cudaSuccess)
-        e = p->bits == 64 ? row_pass_step<float>(p, sub, nullptr, cs) : row_pass_step<double>(p, sub, nullptr, cs);
+        e = by_prec(p->bits, [&](auto t) { return row_pass_step<decltype(t)>(p, sub, nullptr, cs); });
       if (e == cudaSuccess) e = cudaEventRecordWithFlags(ev[4 * i + 3], cs, cudaEventRecordExternal);
       p->form = kMixed;
       p->prev_sub = sub;
@@ -1441,7 +1607,7 @@ int sgpe_device_status(sgpe_plan* p, int* status) {
 }
 
 int sgpe_shape_count(int dtype_bits, int axis, int n) {
-  if ((dtype_bits != 64 && dtype_bits != 128) || (axis != 0 && axis != 1)) return 0;
+  if ((dtype_bits != 64 && dtype_bits != 128 && dtype_bits != SGPE_DTYPE_DF) || (axis != 0 && axis != 1)) return 0;
   return shape_count(dtype_bits, axis, n);
 }
 
@@ -1510,13 +1676,11 @@ int sgpe_autotune(sgpe_plan* p, int n_steps, int* row_shape, int* col_shape, dou
         p->prev_sub = prev0;
         p->pending_pops = nullptr;
         // warm-up: reaches the steady state and captures both step graphs
-        rc = p->bits == 64 ? full_steps_impl<float>(p, kGraphSteps + 2, nullptr, s)
-                           : full_steps_impl<double>(p, kGraphSteps + 2, nullptr, s);
+        rc = by_prec(p->bits, [&](auto t) { return full_steps_impl<decltype(t)>(p, kGraphSteps + 2, nullptr, s); });
         if (rc != SGPE_OK) break;
         e = cudaEventRecord(ev[0], s);
         if (e == cudaSuccess) {
-          rc = p->bits == 64 ? full_steps_impl<float>(p, n_steps, nullptr, s)
-                             : full_steps_impl<double>(p, n_steps, nullptr, s);
+          rc = by_prec(p->bits, [&](auto t) { return full_steps_impl<decltype(t)>(p, n_steps, nullptr, s); });
           if (rc != SGPE_OK) break;
           e = cudaEventRecord(ev[1], s);
         }
@@ -1682,6 +1846,7 @@ void build_groups(sgpe_batch* b) {
     sgpe_plan* p = b->plans[i];
     auto sep = [](const sgpe_plan* q) {
       if (q->tc) return false;  // the grouped kernels carry the FP32 DFTs
+      if (q->bits == SGPE_DTYPE_DF) return false;  // no grouped double-float kernels
       for (int sub = 0; sub < 2; ++sub)
         if (!(q->sub[sub].sep.pot && (!q->coupling || q->sub[sub].sep.cpl))) return false;
       return true;
@@ -1754,7 +1919,7 @@ int capture_batch(sgpe_batch* b, int steps, cudaGraphExec_t* out) {
     sgpe_plan* p = b->plans[i];
     e = cudaStreamWaitEvent(p->cap_stream, b->fork, 0);
     for (int k = 0; k < steps && e == cudaSuccess && rc == SGPE_OK; ++k)
-      rc = p->bits == 64 ? eager_step<float>(p, nullptr, p->cap_stream) : eager_step<double>(p, nullptr, p->cap_stream);
+      rc = by_prec(p->bits, [&](auto t) { return eager_step<decltype(t)>(p, nullptr, p->cap_stream); });
     if (e == cudaSuccess && rc == SGPE_OK) e = cudaEventRecord(b->joins[i], p->cap_stream);
     if (e == cudaSuccess && rc == SGPE_OK) e = cudaStreamWaitEvent(b->root, b->joins[i], 0);
   }
@@ -1801,7 +1966,7 @@ int sgpe_batch_steps(sgpe_batch* b, int n_steps, void* stream) {
     if (!(p->form == kMixed && p->prev_sub == 0 && p->pending_pops == nullptr)) eager = true;
   if (eager && n_steps > 0) {
     for (sgpe_plan* p : b->plans) {
-      const int rc = p->bits == 64 ? eager_step<float>(p, nullptr, s) : eager_step<double>(p, nullptr, s);
+      const int rc = by_prec(p->bits, [&](auto t) { return eager_step<decltype(t)>(p, nullptr, s); });
       if (rc != SGPE_OK) return rc;
     }
     done = 1;
@@ -1828,8 +1993,7 @@ int sgpe_fft2(sgpe_plan* p, const void* i0, const void* i1, void* o0, void* o1, 
   if (p == nullptr || !i0 || !i1 || !o0 || !o1) return fail(SGPE_ERR_ARG, "null plan or data pointer");
   DeviceGuard g(p->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  return p->bits == 64 ? fft2<float>(p, i0, i1, o0, o1, inverse, scale, s)
-                       : fft2<double>(p, i0, i1, o0, o1, inverse, scale, s);
+  return by_iface(p->bits, [&](auto t) { return fft2<decltype(t)>(p, i0, i1, o0, o1, inverse, scale, s); });
 }
 
 }  // extern "C"

@@ -1,0 +1,10 @@
+// Double-float row-pass kernels, separable operators, sides 1024-4096: explicit instantiation.
+#define SGPE_DF_KERNELS
+#define SGPE_INSTANTIATE
+#include "sgpe_launch.cuh"
+
+namespace sgpe {
+template cudaError_t launch_df_row_n<true, 1024>(const RowArgs<DF>&, int, cudaStream_t);
+template cudaError_t launch_df_row_n<true, 2048>(const RowArgs<DF>&, int, cudaStream_t);
+template cudaError_t launch_df_row_n<true, 4096>(const RowArgs<DF>&, int, cudaStream_t);
+}  // namespace sgpe

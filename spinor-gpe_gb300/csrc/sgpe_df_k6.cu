@@ -1,0 +1,10 @@
+// Double-float row-pass kernels, generic operator fields, sides 3 * 2^k: explicit instantiation.
+#define SGPE_DF_KERNELS
+#define SGPE_INSTANTIATE
+#include "sgpe_launch.cuh"
+
+namespace sgpe {
+template cudaError_t launch_df_row_n<false, 192>(const RowArgs<DF>&, int, cudaStream_t);
+template cudaError_t launch_df_row_n<false, 384>(const RowArgs<DF>&, int, cudaStream_t);
+template cudaError_t launch_df_row_n<false, 768>(const RowArgs<DF>&, int, cudaStream_t);
+}  // namespace sgpe

@@ -42,72 +42,21 @@
 #define SGPE_TW_FACTOR 0
 #endif
 
-// Complex128 transforms in double-float arithmetic: the state, the
-// point-wise operators and the reductions stay FP64, while the butterflies
-// of every transform run on FP32 pairs (hi + lo, ~48 significant bits) with
-// head + tail twiddle tables.  (1) on, (0) FP64 butterflies.  Off: measured
-// on GB300 (complex128 imaginary-time steps, default shapes) 64^2 111 ->
-// 117 us, 128^2 125 -> 127 us, 256^2 158 -> 147 us, 512^2 599 -> 458 us,
-// while the transforms' ~48-bit accuracy breaks the original's FFT
-// invariant on an all-ones 256x128 grid (atom number to 10 eps per point:
-// 8.7e-11 against a bound of 7.3e-11).
-#ifndef SGPE_F64_DF
-#define SGPE_F64_DF 0
-#endif
-
 #include <type_traits>
 
+#include "sgpe_df.cuh"
 #include "sgpe_tc.cuh"
 
 namespace sgpe {
 
+// Complex element type of each precision: complex64 (float2), complex128
+// (double2) and double-float (DFC, FP32 head + tail pairs).
 template <typename R> struct CxT;
 template <> struct CxT<float> { using type = float2; };
 template <> struct CxT<double> { using type = double2; };
+template <> struct CxT<DF> { using type = DFC; };
 template <typename R> using Cx = typename CxT<R>::type;
 
-// Double-float scalar: the value hi + lo with |lo| <= ulp(hi)/2.  Sums use
-// Knuth's TwoSum on the heads (the tails added without a second TwoSum, an
-// error of order 2^-47 of the operands' magnitude), products Dekker's
-// exact-product identity through an FMA, each renormalised with
-// FastTwoSum.  FP32 only.
-struct DF {
-  float hi, lo;
-  DF() = default;
-  __host__ __device__ constexpr DF(float h, float l) : hi(h), lo(l) {}
-  __host__ __device__ constexpr explicit DF(double d) : hi(float(d)), lo(float(d - double(float(d)))) {}
-};
-// (the _rn intrinsics keep the compiler from contracting these sequences
-// into FMAs, which would break the error-free transformations)
-__device__ __forceinline__ DF df_fast_two_sum(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  return DF(s, __fsub_rn(b, __fsub_rn(s, a)));
-}
-__device__ __forceinline__ DF operator+(DF a, DF b) {
-  const float s = __fadd_rn(a.hi, b.hi);
-  const float bb = __fsub_rn(s, a.hi);
-  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
-  return df_fast_two_sum(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
-}
-__device__ __forceinline__ DF operator-(DF a) { return DF(-a.hi, -a.lo); }
-__device__ __forceinline__ DF operator-(DF a, DF b) { return a + (-b); }
-__device__ __forceinline__ DF operator*(DF a, DF b) {
-  const float p = __fmul_rn(a.hi, b.hi);
-  float e = __fmaf_rn(a.hi, b.hi, -p);
-  e = __fmaf_rn(a.hi, b.lo, e);
-  e = __fmaf_rn(a.lo, b.hi, e);
-  return df_fast_two_sum(p, e);
-}
-struct DFC {
-  DF x, y;
-};
-__device__ __forceinline__ DF to_df(double d) {
-  const float h = __double2float_rn(d);
-  return DF(h, __double2float_rn(d - double(h)));
-}
-__device__ __forceinline__ double from_df(DF a) { return double(a.hi) + double(a.lo); }
-__device__ __forceinline__ DFC to_dfc(double2 z) { return DFC{to_df(z.x), to_df(z.y)}; }
-__device__ __forceinline__ double2 from_dfc(DFC z) { return make_double2(from_df(z.x), from_df(z.y)); }
 // conversion between a storage complex type CS and a compute type C
 template <class C, class CS> __device__ __forceinline__ C to_compute(CS z) {
   if constexpr (std::is_same<C, CS>::value) return z;
@@ -118,20 +67,21 @@ template <class CS, class C> __device__ __forceinline__ CS to_storage(C z) {
   else return from_dfc(z);
 }
 
-// Element type of the twiddle tables (see SGPE_TW_COMP, SGPE_F64_DF).
+// Element type of the twiddle tables (see SGPE_TW_COMP): double-float
+// transforms read FP32 head + tail entries (hi.x, hi.y, lo.x, lo.y).
 template <typename R> struct TwT { using type = Cx<R>; };
 #if SGPE_TW_COMP
 template <> struct TwT<float> { using type = float4; };
-#endif
-#if SGPE_F64_DF
-template <> struct TwT<double> { using type = float4; };
 #endif
 template <> struct TwT<DF> { using type = float4; };
 template <typename R> using TwE = typename TwT<R>::type;
 
 __device__ __forceinline__ float fmadd(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double fmadd(double a, double b, double c) { return __fma_rn(a, b, c); }
-__device__ __forceinline__ DF fmadd(DF a, DF b, DF c) { return a * b + c; }
+__device__ __forceinline__ DF fmadd(DF a, DF b, DF c) { return df_fma(a, b, c); }
+
+// v or -v for DIR > 0 or DIR < 0 (exact; the same bits as (+-1) * v)
+template <int DIR, class T> __device__ __forceinline__ T sgn(T v) { return DIR < 0 ? -v : v; }
 
 template <class C> __device__ __forceinline__ C cmake(decltype(C::x) a, decltype(C::x) b) {
   C r; r.x = a; r.y = b; return r;
@@ -144,6 +94,13 @@ template <class C> __device__ __forceinline__ C cmul(C a, C b) {
 // a * conj(b)
 template <class C> __device__ __forceinline__ C cmulc(C a, C b) {
   return cmake<C>(fmadd(a.x, b.x, a.y * b.y), fmadd(a.y, b.x, -a.x * b.y));
+}
+// double-float complex products: each part one two-product dot (df_dot2)
+template <> __device__ __forceinline__ DFC cmul<DFC>(DFC a, DFC b) {
+  return DFC{df_dot2<-1>(a.x, b.x, a.y, b.y), df_dot2<1>(a.x, b.y, a.y, b.x)};
+}
+template <> __device__ __forceinline__ DFC cmulc<DFC>(DFC a, DFC b) {
+  return DFC{df_dot2<1>(a.x, b.x, a.y, b.y), df_dot2<-1>(a.y, b.x, a.x, b.y)};
 }
 template <class C> __device__ __forceinline__ C cscale(C a, decltype(C::x) s) { return cmake<C>(a.x * s, a.y * s); }
 
@@ -177,18 +134,18 @@ template <int DIR, int M, class C> __device__ __forceinline__ C tw16(C a) {
   const R c1 = R(0.92387953251128675613);  // cos(pi/8)
   const R s1 = R(0.38268343236508977173);  // sin(pi/8)
   const R h = R(0.70710678118654752440);   // sqrt(1/2)
-  const R d = R(DIR);
+  // products with DIR = +-1 are written as sign changes (same bits)
   if constexpr (m == 0) return a;
   else if constexpr (m == 4) return crot<DIR>(a);
   else if constexpr (m == 8) return cmake<C>(-a.x, -a.y);
   else if constexpr (m == 12) return crot<-DIR>(a);
-  else if constexpr (m == 2) return cscale(cmake<C>(a.x - d * a.y, a.y + d * a.x), h);
-  else if constexpr (m == 6) return cscale(cmake<C>(-a.x - d * a.y, d * a.x - a.y), h);
-  else if constexpr (m == 1) return cmul(a, cmake<C>(c1, d * s1));
-  else if constexpr (m == 3) return cmul(a, cmake<C>(s1, d * c1));
-  else if constexpr (m == 9) return cmul(a, cmake<C>(-c1, -d * s1));
-  else if constexpr (m == 5) return crot<DIR>(cmul(a, cmake<C>(c1, d * s1)));  // W^4 W^1
-  else if constexpr (m == 7) return crot<DIR>(cmul(a, cmake<C>(s1, d * c1)));  // W^4 W^3
+  else if constexpr (m == 2) return cscale(cmake<C>(a.x - sgn<DIR>(a.y), a.y + sgn<DIR>(a.x)), h);
+  else if constexpr (m == 6) return cscale(cmake<C>(-a.x - sgn<DIR>(a.y), sgn<DIR>(a.x) - a.y), h);
+  else if constexpr (m == 1) return cmul(a, cmake<C>(c1, sgn<DIR>(s1)));
+  else if constexpr (m == 3) return cmul(a, cmake<C>(s1, sgn<DIR>(c1)));
+  else if constexpr (m == 9) return cmul(a, cmake<C>(-c1, sgn<-DIR>(s1)));
+  else if constexpr (m == 5) return crot<DIR>(cmul(a, cmake<C>(c1, sgn<DIR>(s1))));  // W^4 W^1
+  else if constexpr (m == 7) return crot<DIR>(cmul(a, cmake<C>(s1, sgn<DIR>(c1))));  // W^4 W^3
   else return crot<DIR>(tw16<DIR, m - 4>(a));                                   // 10, 11, 13, 14, 15
 }
 
@@ -227,11 +184,10 @@ template <int DIR, int M, class C> __device__ __forceinline__ C tw32(C a) {
     const R s1 = R(0.19509032201612826785);  // sin(pi/16)
     const R c3 = R(0.83146961230254523708);  // cos(3 pi/16)
     const R s3 = R(0.55557023301960222474);  // sin(3 pi/16)
-    const R d = R(DIR);
-    if constexpr (m == 1) return cmul(a, cmake<C>(c1, d * s1));
-    else if constexpr (m == 3) return cmul(a, cmake<C>(c3, d * s3));
-    else if constexpr (m == 5) return cmul(a, cmake<C>(s3, d * c3));  // cos(5pi/16) = sin(3pi/16)
-    else return cmul(a, cmake<C>(s1, d * c1));                        // m == 7
+    if constexpr (m == 1) return cmul(a, cmake<C>(c1, sgn<DIR>(s1)));
+    else if constexpr (m == 3) return cmul(a, cmake<C>(c3, sgn<DIR>(s3)));
+    else if constexpr (m == 5) return cmul(a, cmake<C>(s3, sgn<DIR>(c3)));  // cos(5pi/16) = sin(3pi/16)
+    else return cmul(a, cmake<C>(s1, sgn<DIR>(c1)));                        // m == 7
   }
 }
 
@@ -247,8 +203,7 @@ template <int DIR, int M, class C> __device__ __forceinline__ C tw24(C a) {
     // cos and sin of pi m / 12, m = 1..5
     constexpr double kc[6] = {1.0, 0.96592582628906828675, 0.86602540378443864676, 0.70710678118654752440, 0.5,
                               0.25881904510252076235};
-    const R d = R(DIR);
-    return cmul(a, cmake<C>(R(kc[m]), d * R(kc[6 - m])));  // sin(pi m/12) = cos(pi (6-m)/12)
+    return cmul(a, cmake<C>(R(kc[m]), sgn<DIR>(R(kc[6 - m]))));  // sin(pi m/12) = cos(pi (6-m)/12)
   }
 }
 // The same with the exponent known only after unrolling (the switch folds).
@@ -680,35 +635,10 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
 // have synchronised after other threads wrote it, unless each thread wrote
 // only its own positions); with TO_SMEM the output is left there in natural
 // order and `v` is not written.
-// With SGPE_F64_DF, complex128 lines are transformed in double-float
-// arithmetic: the points are split into FP32 heads and tails on entry
-// (registers, or the natural-order line in shared memory), the exchanges
-// carry double-float values, and the result is joined back to FP64 on exit;
-// the twiddle tables are then head + tail entries.
 template <int N, int E, int DIR, int L, bool FROM_SMEM = false, bool TO_SMEM = false, class C, class SM>
 __device__ __forceinline__ void fft_lines(C (&v)[L][E], int j, const SM& sm, const C* __restrict__ tw) {
   static_assert(N % E == 0, "N must be a multiple of E");
-  if constexpr (SGPE_F64_DF && std::is_same<C, double2>::value) {
-    static_assert(!SGPE_TW_FACTOR, "factorised twiddles read plain complex tables");
-    DFC w[L][E];
-    if constexpr (!FROM_SMEM) {
-#pragma unroll
-      for (int l = 0; l < L; ++l)
-#pragma unroll
-        for (int m = 0; m < E; ++m) w[l][m] = to_dfc(v[l][m]);
-    }
-    const auto smd = sm.template retype<DFC>();
-    fft_stage<N, E, DIR, L, 1, FROM_SMEM, TO_SMEM, DFC, decltype(smd), double2>(w, j, smd,
-                                                                              reinterpret_cast<const DFC*>(tw));
-    if constexpr (!TO_SMEM) {
-#pragma unroll
-      for (int l = 0; l < L; ++l)
-#pragma unroll
-        for (int m = 0; m < E; ++m) v[l][m] = from_dfc(w[l][m]);
-    }
-  } else {
-    fft_stage<N, E, DIR, L, 1, FROM_SMEM, TO_SMEM>(v, j, sm, tw);
-  }
+  fft_stage<N, E, DIR, L, 1, FROM_SMEM, TO_SMEM>(v, j, sm, tw);
 }
 
 }  // namespace sgpe

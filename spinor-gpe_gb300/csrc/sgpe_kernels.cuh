@@ -68,6 +68,8 @@
 namespace sgpe {
 
 constexpr int kOpsUnroll = SGPE_OPS_UNROLL;
+// the double-float point-wise loop is long enough without unrolling
+template <typename R> __host__ __device__ constexpr int ops_unroll() { return is_df<R>::value ? 1 : kOpsUnroll; }
 
 // Device error word codes (a kernel that gives up a bounded wait records one
 // and carries on with plain loads).
@@ -122,7 +124,7 @@ template <typename R> struct Field {
   int sx, sy;
 };
 template <typename R> __device__ __forceinline__ Cx<R> fld(const Field<R>& f, int x, int y) {
-  return __ldg(f.p + (x * f.sx + y * f.sy));
+  return ldg(f.p + (x * f.sx + y * f.sy));
 }
 
 // Kinetic propagator exp(-i K_c t/2) = a_c(x, y) * b_c(x, y) in natural k order.
@@ -266,9 +268,10 @@ template <typename R> struct CopyArgs {
 };
 
 // Butterfly (pairwise) sum over a warp.
+template <typename T> __device__ __forceinline__ T shfl_xor(T v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
 template <typename T> __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  for (int o = 16; o > 0; o >>= 1) v = v + shfl_xor(v, o);
   return v;
 }
 
@@ -350,6 +353,28 @@ __device__ __forceinline__ void sum_partials(const float* part, int ntile, int l
   *w = c.value();
 }
 
+// Double-float partials [comp][tile][u, w]: double-float sums in a fixed
+// order (every lane ends with the same bits, as above).
+__device__ __forceinline__ void sum_partials(const DF* part, int ntile, int lane, DF* u0, DF* u1, DF* w) {
+  DF su0(0), su1(0), sw(0);
+  for (int i = lane; i < 2 * ntile; i += 32) {
+    const float4 uw = reinterpret_cast<const float4*>(part)[i];
+    sw += DF(uw.z, uw.w);
+    if (i < ntile) su0 += DF(uw.x, uw.y); else su1 += DF(uw.x, uw.y);
+  }
+  *u0 = warp_sum(su0);
+  *u1 = warp_sum(su1);
+  *w = warp_sum(sw);
+}
+__device__ __forceinline__ void sum_partials(const DF* part, int ntile, int lane, double* u0, double* u1,
+                                             double* w) {
+  DF a, b, c;
+  sum_partials(part, ntile, lane, &a, &b, &c);
+  *u0 = from_df(a);
+  *u1 = from_df(b);
+  *w = from_df(c);
+}
+
 // lambda = sqrt(num / w) of the row pass, in the working precision.
 __device__ __forceinline__ float row_lambda(const float* part, int ntile, int lane, float norm_num, double* u0,
                                             double* u1, bool want_u) {
@@ -366,6 +391,18 @@ __device__ __forceinline__ double row_lambda(const double* part, int ntile, int 
   double sw;
   sum_partials(part, ntile, lane, u0, u1, &sw);
   return sqrt(norm_num / sw);
+}
+// double-float: the sums in double-float, the square root of the quotient in
+// FP64 (a few FP64 operations per block) rounded to a double-float value
+__device__ __forceinline__ DF row_lambda(const DF* part, int ntile, int lane, DF norm_num, double* u0, double* u1,
+                                         bool want_u) {
+  DF a, b, c;
+  sum_partials(part, ntile, lane, &a, &b, &c);
+  if (want_u) {
+    *u0 = from_df(a);
+    *u1 = from_df(b);
+  }
+  return to_df(sqrt(from_df(norm_num) / from_df(c)));
 }
 
 // Sum of |v[m]|^2 over the E points of a thread, pairwise in the working
@@ -412,6 +449,8 @@ __device__ __forceinline__ void sin_cos_phase(float x, float* s, float* c) {
   }
 }
 __device__ __forceinline__ void sin_cos_phase(double x, double* s, double* c) { sincos(x, s, c); }
+__device__ __forceinline__ void sin_cos_phase(DF x, DF* s, DF* c) { df_sincos(x, s, c); }
+__device__ __forceinline__ DF exp_r(DF x) { return df_exp(x); }
 
 // exp(z * e) for the interaction operator.
 template <typename R> __device__ __forceinline__ Cx<R> cexp_z(R zr, R zi, R e) {
@@ -519,14 +558,14 @@ template <typename R, int E, int T>
 __device__ __forceinline__ void apply_kinetic(Cx<R> (&v)[E], const KinOp<R>& k, int comp, int x, int j) {
   using C = Cx<R>;
   if (k.sep) {  // x-table times y-table, unit strides
-    const C ka = __ldg(k.a[comp].p + x);
+    const C ka = ldg(k.a[comp].p + x);
     const C* kb = k.b[comp].p + j;
     if (k.real) {  // same bits as the complex products (see apply_real_ops)
 #pragma unroll
-      for (int m = 0; m < E; ++m) v[m] = cscale(v[m], ka.x * __ldg(&kb[m * T].x));
+      for (int m = 0; m < E; ++m) v[m] = cscale(v[m], ka.x * ldg(&kb[m * T].x));
     } else {
 #pragma unroll
-      for (int m = 0; m < E; ++m) v[m] = cmul(v[m], cmul(ka, __ldg(kb + m * T)));
+      for (int m = 0; m < E; ++m) v[m] = cmul(v[m], cmul(ka, ldg(kb + m * T)));
     }
     return;
   }
@@ -683,22 +722,22 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
         // separable operators: x-tables read at jj + m*2T (compile-time
         // offsets from one base), row values and the uniform c hoisted
         PointOps<R> v;
-        v.pb0 = __ldg(a.op.pb[0].p + y);
-        v.pb1 = __ldg(a.op.pb[1].p + y);
-        v.cc = a.coupling ? __ldg(a.op.cc.p) : C{};
+        v.pb0 = ldg(a.op.pb[0].p + y);
+        v.pb1 = ldg(a.op.pb[1].p + y);
+        v.cc = a.coupling ? ldg(a.op.cc.p) : C{};
         const C* pa0 = a.op.pa[0].p + jj;
         const C* pa1 = a.op.pa[1].p + jj;
         const C* s01 = a.op.s01.p + jj;
         const C* s10 = a.op.s10.p + jj;
-#pragma unroll kOpsUnroll
+#pragma unroll ops_unroll<R>()
         for (int m = 0; m < E / 2; ++m) {
           const int x = jj + m * 2 * T;
           C p0 = cscale(at0(m, x), lam), p1 = cscale(at1(m, x), lam);
-          v.pa0 = __ldg(pa0 + m * 2 * T);
-          v.pa1 = __ldg(pa1 + m * 2 * T);
+          v.pa0 = ldg(pa0 + m * 2 * T);
+          v.pa1 = ldg(pa1 + m * 2 * T);
           if (a.coupling) {
-            v.s01 = __ldg(s01 + m * 2 * T);
-            v.s10 = __ldg(s10 + m * 2 * T);
+            v.s01 = ldg(s01 + m * 2 * T);
+            v.s10 = ldg(s10 + m * 2 * T);
           }
           apply_real_ops<R>(p0, p1, v, a);
           at0(m, x) = p0;
@@ -707,7 +746,7 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
       } else {
         RowFields<R> rf;
         rf.init(a.op, y);
-#pragma unroll kOpsUnroll
+#pragma unroll ops_unroll<R>()
         for (int m = 0; m < E / 2; ++m) {
           const int x = jj + m * 2 * T;
           C p0 = cscale(at0(m, x), lam), p1 = cscale(at1(m, x), lam);
@@ -954,5 +993,21 @@ __global__ void __launch_bounds__(256) copy_kernel(const CopyArgs<R> a) {
     a.out[1][i] = cscale(a.in[1][src], a.scale);
   }
 }
+
+// Conversion copies of a double-float plan's state: complex128 psik into
+// the double-float state (load), and the double-float state out to complex128
+// (store), with the fftshift of psik's centred order and, on store, the final
+// k-space renormalisation from the column pass's partials.
+struct DfCopyArgs {
+  const void* in[2];
+  void* out[2];
+  int nx, ny;
+  int shift;            // out = fftshift(in) in both axes (even sizes)
+  int to_df;            // 1: double2 -> DFC, 0: DFC -> double2
+  const DF* part;       // non-null (store): renormalise with these partials
+  int ntile;
+  double atom_num, dv;
+  double* pops;         // non-null (store): populations
+};
 
 }  // namespace sgpe

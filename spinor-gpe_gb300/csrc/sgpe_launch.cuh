@@ -1,8 +1,8 @@
 // Launch configuration and size dispatch for the split-step kernels.
 //
 // Line lengths are compile-time: every power of two from 32 to 4096, and 192,
-// 384 and 768, along either axis, instantiated for complex64 (float) and
-// complex128 (double).
+// 384 and 768, along either axis, instantiated for complex64 (float),
+// complex128 (double) and double-float (DF, kernel shape 0 only).
 #pragma once
 #include "sgpe_kernels.cuh"
 
@@ -73,6 +73,28 @@ template <> struct Tune<double> {
   static constexpr int R3_E = 12, R3_ROW_MINB = 2, R3_COL_MINB = 1;
   static constexpr int R3_E_LARGE = 12, R3_COL_MINB_LARGE = 1;
 };
+// Double-float: a complex value is four FP32 registers, so 8 points per
+// thread (12 for sides 3 * 2^k), 128-register caps (two 256-thread blocks
+// per SM), 4-column tiles (64-byte row segments, as complex128).
+#ifndef SGPE_DF_ROW_THREADS
+#define SGPE_DF_ROW_THREADS 256
+#endif
+#ifndef SGPE_DF_ROW_MINB
+#define SGPE_DF_ROW_MINB 2
+#endif
+#ifndef SGPE_DF_COLS
+#define SGPE_DF_COLS 4
+#endif
+#ifndef SGPE_DF_COL_MINB
+#define SGPE_DF_COL_MINB 1
+#endif
+template <> struct Tune<DF> {
+  static constexpr int ROW_E = 8, ROW_THREADS = SGPE_DF_ROW_THREADS, ROW_MINB = SGPE_DF_ROW_MINB;
+  static constexpr int ROW_E_LARGE = 8, ROW_MINB_LARGE = SGPE_DF_ROW_MINB;
+  static constexpr int COL_E = 8, COLS = SGPE_DF_COLS, COL_MINB = SGPE_DF_COL_MINB;
+  static constexpr int R3_E = 12, R3_ROW_MINB = SGPE_DF_ROW_MINB, R3_COL_MINB = SGPE_DF_COL_MINB;
+  static constexpr int R3_E_LARGE = 12, R3_COL_MINB_LARGE = SGPE_DF_COL_MINB;
+};
 
 constexpr int cmin(int a, int b) { return a < b ? a : b; }
 constexpr int cmax(int a, int b) { return a > b ? a : b; }
@@ -122,6 +144,16 @@ template <> struct ShapeTune<double> {
   static constexpr int row_threads(int, int s) { return s == 2 ? 128 : Tune<double>::ROW_THREADS; }
   static constexpr int col_e(int, int) { return 4; }
   static constexpr int cols(int, int s) { return s == 2 ? 2 : Tune<double>::COLS; }
+};
+// double-float: kernel shape 0 only
+template <> struct ShapeTune<DF> {
+  static constexpr int row_shapes(int) { return 1; }
+  static constexpr int col_shapes(int) { return 1; }
+  static constexpr int row_e(int, int) { return 8; }
+  static constexpr int row_minb(int, int) { return 0; }
+  static constexpr int row_threads(int, int) { return Tune<DF>::ROW_THREADS; }
+  static constexpr int col_e(int, int) { return 8; }
+  static constexpr int cols(int, int) { return Tune<DF>::COLS; }
 };
 template <typename R> constexpr int row_shape_count(int n) { return ShapeTune<R>::row_shapes(n); }
 template <typename R> constexpr int col_shape_count(int n) { return ShapeTune<R>::col_shapes(n); }
@@ -253,6 +285,34 @@ template <typename R, int S> struct ColLauncher {
   }
 };
 
+// Double-float kernels are heavy to compile: the kernels of each size are
+// launched through the function templates below, which are defined only in
+// the sgpe_df_k*.cu translation units (SGPE_DF_KERNELS) and explicitly
+// instantiated there, a few sizes per unit, so the build compiles them in
+// parallel; every other unit sees only their declarations.
+template <bool SEP, int N> cudaError_t launch_df_row_n(const RowArgs<DF>& a, int ny, cudaStream_t s);
+template <int N> cudaError_t launch_df_col_n(const ColArgs<DF>& a, int ny, cudaStream_t s);
+#ifdef SGPE_DF_KERNELS
+template <bool SEP, int N> cudaError_t launch_df_row_n(const RowArgs<DF>& a, int ny, cudaStream_t s) {
+  return RowLauncher<DF, SEP, 0>{&a, ny, s}.template run<N>();
+}
+template <int N> cudaError_t launch_df_col_n(const ColArgs<DF>& a, int ny, cudaStream_t s) {
+  return ColLauncher<DF, 0>{&a, ny, s}.template run<N>();
+}
+#endif
+template <bool SEP> struct DfRowDispatch {
+  const RowArgs<DF>* a;
+  int ny;
+  cudaStream_t s;
+  template <int N> cudaError_t run() const { return launch_df_row_n<SEP, N>(*a, ny, s); }
+};
+struct DfColDispatch {
+  const ColArgs<DF>* a;
+  int ny;
+  cudaStream_t s;
+  template <int N> cudaError_t run() const { return launch_df_col_n<N>(*a, ny, s); }
+};
+
 // Tensor-core DFT16 variant (complex64; sides with radix-16 stages:
 // 64, 256, 1024, 2048).  Rows: the row configuration with a 128-register
 // cap; columns: 4 columns per block (at least one warp), so the staging
@@ -329,6 +389,8 @@ cudaError_t launch_row_tc(const RowArgs<float>& a, int nx, int ny, cudaStream_t 
 cudaError_t launch_col_tc(const ColArgs<float>& a, int ny, cudaStream_t s);
 inline cudaError_t launch_row_tc(const RowArgs<double>&, int, int, cudaStream_t) { return cudaErrorInvalidValue; }
 inline cudaError_t launch_col_tc(const ColArgs<double>&, int, cudaStream_t) { return cudaErrorInvalidValue; }
+inline cudaError_t launch_row_tc(const RowArgs<DF>&, int, int, cudaStream_t) { return cudaErrorInvalidValue; }
+inline cudaError_t launch_col_tc(const ColArgs<DF>&, int, cudaStream_t) { return cudaErrorInvalidValue; }
 
 struct ColTcColsQuery {
   int* out;
@@ -387,10 +449,12 @@ template <typename R, int S> struct ColGroupedLauncher {
 // Per-shape launch functions, explicitly instantiated in their own
 // translation units (shape 0 with the default kernels, shapes 1-2 together).
 template <typename R, bool SEP, int S> cudaError_t launch_row_ops_s(const RowArgs<R>& a, int nx, int ny, cudaStream_t s) {
-  return dispatch_n(nx, RowLauncher<R, SEP, S>{&a, ny, s});
+  if constexpr (is_df<R>::value) return dispatch_n(nx, DfRowDispatch<SEP>{&a, ny, s});
+  else return dispatch_n(nx, RowLauncher<R, SEP, S>{&a, ny, s});
 }
 template <typename R, int S> cudaError_t launch_col_s(const ColArgs<R>& a, int ny, cudaStream_t s) {
-  return dispatch_n(ny, ColLauncher<R, S>{&a, ny, s});
+  if constexpr (is_df<R>::value) return dispatch_n(ny, DfColDispatch{&a, ny, s});
+  else return dispatch_n(ny, ColLauncher<R, S>{&a, ny, s});
 }
 template <typename R, int S>
 cudaError_t launch_row_grouped_s(const RowArgs<R>* args, int groups, int nx, int ny, cudaStream_t s) {
@@ -412,14 +476,22 @@ cudaError_t launch_col_grouped_s(const ColArgs<R>* args, int groups, int nx, int
 // Row kernels with the separable (SEP) or the generic point-wise code, in
 // the shape a.shape.
 template <typename R, bool SEP> cudaError_t launch_row_ops(const RowArgs<R>& a, int nx, int ny, cudaStream_t s) {
-  SGPE_SHAPE_SWITCH(a.shape, (launch_row_ops_s<R, SEP, 0>(a, nx, ny, s)), (launch_row_ops_s<R, SEP, 1>(a, nx, ny, s)),
-                    (launch_row_ops_s<R, SEP, 2>(a, nx, ny, s)))
+  if constexpr (is_df<R>::value) {
+    return a.shape == 0 ? launch_row_ops_s<R, SEP, 0>(a, nx, ny, s) : cudaErrorInvalidValue;
+  } else {
+    SGPE_SHAPE_SWITCH(a.shape, (launch_row_ops_s<R, SEP, 0>(a, nx, ny, s)), (launch_row_ops_s<R, SEP, 1>(a, nx, ny, s)),
+                      (launch_row_ops_s<R, SEP, 2>(a, nx, ny, s)))
+  }
 }
 
 template <typename R> cudaError_t launch_col(const ColArgs<R>& a, int ny, cudaStream_t s) {
   if (a.tc) return launch_col_tc(a, ny, s);
-  SGPE_SHAPE_SWITCH(a.shape, (launch_col_s<R, 0>(a, ny, s)), (launch_col_s<R, 1>(a, ny, s)),
-                    (launch_col_s<R, 2>(a, ny, s)))
+  if constexpr (is_df<R>::value) {
+    return a.shape == 0 ? launch_col_s<R, 0>(a, ny, s) : cudaErrorInvalidValue;
+  } else {
+    SGPE_SHAPE_SWITCH(a.shape, (launch_col_s<R, 0>(a, ny, s)), (launch_col_s<R, 1>(a, ny, s)),
+                      (launch_col_s<R, 2>(a, ny, s)))
+  }
 }
 
 // `args` in device memory, `groups` solves of an (ny, nx) grid, all in the
@@ -511,6 +583,9 @@ SGPE_EXTERN_SHAPE(double, 0)
 SGPE_EXTERN_SHAPE(double, 1)
 SGPE_EXTERN_SHAPE(double, 2)
 #undef SGPE_EXTERN_SHAPE
+extern template cudaError_t launch_row_ops_s<DF, true, 0>(const RowArgs<DF>&, int, int, cudaStream_t);
+extern template cudaError_t launch_row_ops_s<DF, false, 0>(const RowArgs<DF>&, int, int, cudaStream_t);
+extern template cudaError_t launch_col_s<DF, 0>(const ColArgs<DF>&, int, cudaStream_t);
 #endif
 
 // Row pass: the separable kernels unless the step uses generic operator

@@ -80,7 +80,7 @@ int scratch_address(int* dev_out, void** out) {
 // (r - 1) ns + k.  FP64 sincospi of the exactly reduced fraction, rounded once.
 __device__ __forceinline__ void set_twiddle(float2& w, double re, double im) { w = make_float2(float(re), float(im)); }
 __device__ __forceinline__ void set_twiddle(double2& w, double re, double im) { w = make_double2(re, im); }
-#if SGPE_TW_COMP || SGPE_F64_DF
+#if SGPE_TW_COMP
 __device__ __forceinline__ void set_twiddle(float4& w, double re, double im) {
   const float hr = float(re), hi = float(im);
   w = make_float4(hr, hi, float(re - double(hr)), float(im - double(hi)));

@@ -33,6 +33,8 @@ EXPORTED = ('sgpe_version', 'sgpe_last_error', 'sgpe_plan_create',
             'sgpe_autotune', 'sgpe_device_status', 'sgpe_check_bounded_wait')
 
 SGPE_MAX_SHAPES = 3
+# dtype_bits of the double-float precision (include/spinor_gb300.h)
+SGPE_DTYPE_DF = 48
 
 
 class SgpeError(RuntimeError):

@@ -11,7 +11,10 @@ that is not a CUDA device raises.
 Differences a caller can observe:
 
 * ``device`` defaults to ``'cuda'``; ``dtype`` (64 or 128, default 128) selects
-  complex64 or complex128 arithmetic.
+  complex64 or complex128 arithmetic; ``dtype='double-float'`` keeps the
+  state, the operator tables and every transform in pairs of FP32 values
+  (about 48 significant bits on the FP32 pipes), with ``psik`` in
+  complex128.
 * ``psik`` is materialised on read from the device state (functional, as in
   the original, which rebinds ``self.psik`` every sub-step); assigning it loads
   a new state.
@@ -46,7 +49,10 @@ def _bits(dtype):
         return 64
     if dtype in (128, 'complex128', torch.complex128, np.complex128):
         return 128
-    raise ValueError(f'dtype must be complex64 or complex128, got {dtype!r}')
+    if dtype in (_native.SGPE_DTYPE_DF, 'double-float', 'df'):
+        return _native.SGPE_DTYPE_DF
+    raise ValueError("dtype must be complex64, complex128 or 'double-float', "
+                     f"got {dtype!r}")
 
 
 def cuda_device(device):
@@ -119,7 +125,7 @@ class TensorPropagator:
 
     Parameters follow ``tensor_propagator.py:67-91``: ``spin`` (a
     ``PSpinor``), ``t_step``, ``n_steps``, ``device``, ``time`` ('imag' or
-    'real'), ``is_sampling``, ``n_samples``; plus ``dtype`` (64 / 128) and
+    'real'), ``is_sampling``, ``n_samples``; plus ``dtype`` (64 / 128 / 'double-float') and
     ``tensor_core_dft`` (complex64 only: radix-16 DFT stages as split-BF16
     products on the tensor cores, a precision-study variant),
     ``kernel_shapes`` (row and column kernel shapes, default: the shapes

@@ -69,6 +69,9 @@ def parse():
     ap.add_argument('--serve-rate', type=float, default=200.0)
     ap.add_argument('--serve-window', type=float, default=0.5)
     ap.add_argument('--max-active', type=int, default=64)
+    ap.add_argument('--dtype', default='64', choices=['64', '128', 'double-float'],
+                    help='raman_quench: precision of the timed solves (complex64, '
+                         'complex128, or double-float: FP32 head + tail pairs)')
     ap.add_argument('--tensor-core-dft', action='store_true',
                     help='raman_quench: run the split-BF16 tensor-core DFT16 '
                          'variant (precision study; not the headline)')
@@ -272,13 +275,16 @@ def run_native(args, world, rank, local):
     n = args.n
     tmp = tempfile.mkdtemp(prefix='sgpe_bench_')
     ps = build_problem(tmp, n, args.prep_steps, device)
-    state_bytes = 2 * n * n * 8
+    dtype = args.dtype if args.dtype == 'double-float' else int(args.dtype)
+    elem = 8 if dtype == 64 else 16       # bytes per complex value of the state
+    host_ctype = torch.complex64 if dtype == 64 else torch.complex128
+    state_bytes = 2 * n * n * elem
     n_rep = max(1, math.ceil(2 * L2_BYTES / state_bytes) + 1)
-    psik_host = [torch.as_tensor(np.asarray(p), dtype=torch.complex64)
+    psik_host = [torch.as_tensor(np.asarray(p), dtype=host_ctype)
                  .pin_memory() for p in ps.psik]
     shapes = tuple(args.kernel_shapes) if args.kernel_shapes else None
     props = [tprop.TensorPropagator(ps, 1e-3, args.steps, device, time='real',
-                                    dtype=64, tensor_core_dft=args.tensor_core_dft,
+                                    dtype=dtype, tensor_core_dft=args.tensor_core_dft,
                                     kernel_shapes=shapes)
              for _ in range(n_rep)]
     stream = torch.cuda.current_stream()
@@ -330,7 +336,7 @@ def run_native(args, world, rank, local):
     pops_dev = [torch.empty((k, 2), dtype=torch.float64, device=device)
                 for _ in range(n_rep)]
     pops_host = torch.empty((k, 2), dtype=torch.float64).pin_memory()
-    out_host = [[torch.empty((n, n), dtype=torch.complex64).pin_memory()
+    out_host = [[torch.empty((n, n), dtype=host_ctype).pin_memory()
                  for _ in range(2)] for _ in range(n_rep)]
     barrier(world)
     torch.cuda.synchronize()
@@ -353,10 +359,10 @@ def run_native(args, world, rank, local):
     assert np.isfinite(out_host[0][0].numpy()).all()
 
     peak, peak_kind = measured_peaks()
-    pass_bytes = 4 * n * n * 8            # read + write of both components
+    pass_bytes = 4 * n * n * elem         # read + write of both components
     dom_ms, dom_name = max((row_ms, 'row_kernel'), (col_ms, 'col_kernel'))
     achieved = pass_bytes / (dom_ms / 1e3) / 1e9
-    step_bytes = 48 * n * n * 8           # 12 sweeps per full step (reference count)
+    step_bytes = 48 * n * n * elem        # 12 sweeps per full step (reference count)
     traffic = None
     tpath = os.path.join(REPO, 'profiles', 'traffic.json')
     if os.path.exists(tpath):
@@ -375,7 +381,9 @@ def run_native(args, world, rank, local):
         'ms_per_step': 1e3 * t_max / k * 1.0,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': ('c64 (split-BF16 tensor-core DFT16 stages)' if args.tensor_core_dft
-                  else 'c64 (fp32 butterflies; fp64 reductions)'),
+                  else 'c64 (fp32 butterflies; fp64 reductions)' if dtype == 64
+                  else 'c128 (fp64)' if dtype == 128
+                  else 'double-float (fp32 head + tail pairs, ~48 bits; fp64 reductions)'),
         'data': 'synthetic (seeded Thomas-Fermi + phase noise, 3000-step '
                 'imaginary-time preparation)',
         'config': {'workload': f'raman_quench_{n}', 'grid': [n, n],

@@ -20,7 +20,8 @@ solver's steps/s.
   oracle every 500 steps over the whole run (the quench: 3000 imaginary
   steps, then 10000 real-time steps, each implementation continuing from
   its own ground state; the vortex start: 2000 imaginary steps), for the
-  solver in each precision, the original's own complex64 arithmetic, and
+  solver in each precision (complex64, complex128, double-float), the
+  original's own complex64 arithmetic, and
   two diagnostic complex128 oracle runs that isolate one FP32 effect each:
   the state rounded to complex64 after every sub-step (FP32 storage alone),
   and the operator tables rounded to complex64 (FP32 tables alone).  Besides
@@ -273,6 +274,7 @@ def curve_runners(variants):
             lambda: OracleRunner(RoundedTablesOracle),
         'solver complex64': lambda: SolverRunner(64),
         'solver complex128': lambda: SolverRunner(128),
+        'solver double-float': lambda: SolverRunner('double-float'),
     }
     return [('oracle complex128', OracleRunner())] + [(v, table[v]()) for v in variants]
 
@@ -280,7 +282,7 @@ def curve_runners(variants):
 CURVE_VARIANTS = ['original complex64',
                   'oracle complex128, state rounded to complex64 each sub-step',
                   'oracle complex128, operator tables rounded to complex64',
-                  'solver complex64', 'solver complex128']
+                  'solver complex64', 'solver complex128', 'solver double-float']
 
 
 def curve_quench_1024(tmp, variants=None):

@@ -62,6 +62,12 @@ def parse():
                          'request stream through the continuous-batching loop '
                          'against the same requests solved one after another)')
     ap.add_argument('--solves', type=int, default=96)
+    ap.add_argument('--batch-extra-steps', type=int, default=50,
+                    help='raman_quench: also time the batched uneven solves for this '
+                         'many steps (0: skip) and report them in the same line')
+    ap.add_argument('--precision-modes', nargs='*', default=['double-float', '128'],
+                    help='raman_quench: also time these precisions on the same '
+                         'workload and report them in the same line')
     ap.add_argument('--breakdown', action='store_true',
                     help='batched_uneven: also time each grid-size class alone '
                          '(one solve, the class sequentially, the class batched)')
@@ -69,6 +75,12 @@ def parse():
     ap.add_argument('--serve-rate', type=float, default=200.0)
     ap.add_argument('--serve-window', type=float, default=0.5)
     ap.add_argument('--max-active', type=int, default=64)
+    ap.add_argument('--serve-max-queue', type=float, default=None,
+                    help='served: shed requests that waited longer than this many '
+                         'seconds for admission (default: never shed)')
+    ap.add_argument('--serve-seq-sample', type=int, default=0,
+                    help='served: run the sequential baseline on a seeded sample of '
+                         'this many served requests (0: all of them)')
     ap.add_argument('--dtype', default='64', choices=['64', '128', 'double-float'],
                     help='raman_quench: precision of the timed solves (complex64, '
                          'complex128, or double-float: FP32 head + tail pairs)')
@@ -267,6 +279,39 @@ def torch_cuda_reference_rate(inp, steps=30, warmup=3, dtype=64):
 
 # --------------------------------------------------------------- native arm
 
+def precision_mode_rate(ps, mode, n, device, world, k, warmup):
+    """Full steps/s of the same workload in another precision: replicas
+    stepped round-robin as in the headline (inputs larger than L2), CUDA
+    events on the stream, every replica warmed into graph replay first."""
+    import torch
+    from spinor_gpe.pspinor import tensor_propagator as tprop
+    dtype = mode if mode == 'double-float' else int(mode)
+    elem = 8 if dtype == 64 else 16
+    n_rep = max(1, math.ceil(2 * L2_BYTES / (2 * n * n * elem)) + 1)
+    props = [tprop.TensorPropagator(ps, 1e-3, k, device, time='real', dtype=dtype)
+             for _ in range(n_rep)]
+    for _ in range(3):
+        for p in props:
+            p.full_steps(1)
+    for i in range(warmup):
+        props[i % n_rep].full_steps(1)
+    stream = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for i in range(k):
+        props[i % n_rep].full_steps(1)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t = max_over_ranks(ev0.elapsed_time(ev1) / 1e3, world)
+    del props
+    return {'value': world * k / t, 'unit': UNIT, 'steps': k, 'replicas': n_rep,
+            'dtype': {'double-float': 'double-float (fp32 head + tail pairs, ~48 bits)',
+                      '128': 'c128 (fp64)', '64': 'c64'}[str(mode)]}
+
+
+
 def run_native(args, world, rank, local):
     import torch
     from spinor_gpe.pspinor import tensor_propagator as tprop
@@ -364,16 +409,41 @@ def run_native(args, world, rank, local):
     achieved = pass_bytes / (dom_ms / 1e3) / 1e9
     step_bytes = 48 * n * n * elem        # 12 sweeps per full step (reference count)
     traffic = None
+    traffic_note = None
     tpath = os.path.join(REPO, 'profiles', 'traffic.json')
     if os.path.exists(tpath):
         try:
-            traffic = json.load(open(tpath)).get(dom_name)
+            tj = json.load(open(tpath))
+            traffic = tj.get(dom_name)
+            traffic_note = tj.get('note')
         except ValueError:
             traffic = None
+
+    # the other precisions on the same workload (fewer timed steps)
+    modes = {}
+    for mode in args.precision_modes:
+        modes[mode] = precision_mode_rate(ps, mode, n, device, world,
+                                          max(20, k // 5), args.warmup)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu, _ = cpu_reference_rate(ps)
+
+    shapes0 = list(props[0].kernel_shapes)
+    batched = None
+    if args.batch_extra_steps > 0:
+        del props
+        b = measure_batched(world, rank, local, args.solves, args.batch_extra_steps,
+                            args.warmup)
+        batched = {'value': b['value'], 'unit': b['unit'],
+                   'sequential_plain': b['sequential_plain']['value'],
+                   'speedup_vs_sequential': b['speedup_vs_sequential'],
+                   'solves': args.solves, 'steps': args.batch_extra_steps,
+                   'what': 'the batched uneven ground states (sides 128-1024, '
+                           'seeded parameters, complex64) advanced together by '
+                           'PropagatorBatch (autotuned kernel shapes) against the '
+                           'same solves one after another (bench.py --workload '
+                           'batched_uneven runs it alone)'}
 
     line = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world,
@@ -390,7 +460,7 @@ def run_native(args, world, rank, local):
                    'time': 'real', 'dt': 1e-3, 'delta': 0.5, 'omega': 1.0,
                    'k_L': 3.0, 'g': [1000.0, 1000.0, 990.0],
                    'replicas_per_gpu': n_rep,
-                   'kernel_shapes': list(props[0].kernel_shapes),
+                   'kernel_shapes': shapes0,
                    'l2': f'inputs larger than L2: {n_rep} replica states of '
                          f'{state_bytes >> 20} MiB stepped round-robin',
                    'parallelism': f'replicas x{world}'},
@@ -407,6 +477,7 @@ def run_native(args, world, rank, local):
         'roofline': {'bound': 'hbm', 'kernel': dom_name,
                      'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                      'frac': achieved / peak, 'traffic': traffic,
+                     'traffic_source': traffic_note,
                      'peak_kind': peak_kind,
                      'algorithmic_bytes': pass_bytes,
                      'col_pass_ms': col_ms, 'row_pass_ms': row_ms},
@@ -417,6 +488,10 @@ def run_native(args, world, rank, local):
         'gpu_launches': 6 * k,
         'clocks': clk.summary(),
     }
+    if modes:
+        line['precision_modes'] = modes
+    if batched is not None:
+        line['batched_uneven'] = batched
     if cpu is not None:
         line['cpu_baseline'] = cpu
     if rank == 0:
@@ -431,6 +506,16 @@ def run_batched(args, world, rank, local):
     solves advanced together through ``PropagatorBatch`` (one CUDA graph with
     a branch per solve), against the plain single-solve drop-in stepping the
     same solves one after another.  Metric: aggregate grid-point-steps/s."""
+    line = measure_batched(world, rank, local, args.solves, args.batch_steps,
+                           args.warmup, not args.no_batch_autotune, args.breakdown)
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def measure_batched(world, rank, local, n_solves, k, warmup, autotune=True,
+                    with_breakdown=False):
+    """The batched-uneven measurement (see ``run_batched``); returns its JSON
+    line as a dict."""
     import torch
     from spinor_gpe import workloads
     from spinor_gpe.batch import PropagatorBatch
@@ -441,8 +526,7 @@ def run_batched(args, world, rank, local):
     device = f'cuda:{local}'
     tmp = tempfile.mkdtemp(prefix='sgpe_batch_')
     spins = workloads.batched_uneven(spin.PSpinor, ttools.fft_2d, tmp + '/',
-                                     n_solves=args.solves, seed=4 + rank)
-    k = args.batch_steps
+                                     n_solves=n_solves, seed=4 + rank)
     props = [tprop.TensorPropagator(s, 0.02, k, device, time='imag', dtype=64)
              for s in spins]
     points = sum(s.psik[0].size for s in spins)
@@ -462,11 +546,11 @@ def run_batched(args, world, rank, local):
 
     # plain solves one after another (warm-up captures each plan's graphs)
     for p in props:
-        p.full_steps(max(args.warmup, 9))
+        p.full_steps(max(warmup, 9))
     t_seq = timed(lambda: [p.full_steps(k) for p in props])
 
     breakdown = None
-    if args.breakdown:
+    if with_breakdown:
         breakdown = {}
         kb = max(20, k // 10)
         for n in sorted({s.psik[0].shape[0] for s in spins}):
@@ -482,7 +566,7 @@ def run_batched(args, world, rank, local):
 
     batch = PropagatorBatch(props)
     tuned = None
-    if not args.no_batch_autotune:
+    if autotune:
         # kernel shapes per size class for grouped stepping (set-up, untimed)
         t0 = time.perf_counter()
         tuned = batch.autotune()
@@ -492,7 +576,7 @@ def run_batched(args, world, rank, local):
                 shapes = props[[p._shape[1] for p in props].index(nx)].kernel_shapes
                 breakdown[str(nx)]['batched_tuned_us'] = times[shapes]
                 breakdown[str(nx)]['tuned_shapes'] = list(shapes)
-    batch.full_steps(max(args.warmup, 9))
+    batch.full_steps(max(warmup, 9))
     with ClockSampler(local) as clk:
         t_bat = timed(lambda: batch.full_steps(k))
     for p in props[:4]:
@@ -506,13 +590,13 @@ def run_batched(args, world, rank, local):
         'metric': 'grid-point-steps/s, batched uneven imaginary-time solves '
                   '(complex64)',
         'value': value, 'unit': 'grid-point-steps/s', 'n_gpus': world,
-        'steps': k, 'warmup': max(args.warmup, 9), 'ms_per_step': 1e3 * t_bat / k,
+        'steps': k, 'warmup': max(warmup, 9), 'ms_per_step': 1e3 * t_bat / k,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'c64 (fp32 butterflies; fp64 reductions)',
         'data': 'synthetic (seeded sizes and parameters, Thomas-Fermi + '
                 'phase noise)',
-        'config': {'workload': f'batched_uneven_{args.solves}',
-                   'solves_per_gpu': args.solves, 'grid_sides': sizes,
+        'config': {'workload': f'batched_uneven_{n_solves}',
+                   'solves_per_gpu': n_solves, 'grid_sides': sizes,
                    'grid_points_per_gpu': points, 'dt': 0.02, 'time': 'imag',
                    'l2': f'inputs larger than L2: {points * 16 >> 20} MiB of '
                          f'state per GPU',
@@ -526,13 +610,12 @@ def run_batched(args, world, rank, local):
             f'{ny}x{nx}': list(props[[p._shape for p in props].index((ny, nx))].kernel_shapes)
             for (_, ny, nx) in tuned}),
         'batch_autotune_s': None if tuned is None else tune_s,
-        'gpu_launches': 6 * k * args.solves,
+        'gpu_launches': 6 * k * n_solves,
         'per_class_step_us': breakdown,
         'clocks': clk.summary(),
     }
     batch.close()
-    if rank == 0:
-        print(json.dumps(line))
+    return line
 
 
 # ------------------------------------------------------ served request stream
@@ -559,19 +642,33 @@ def run_served(args, world, rank, local):
     serve.SolveServer(device, max_active=2).run(reqs[:1], realtime=False)
     barrier(world)
     torch.cuda.synchronize()
-    srv = serve.SolveServer(device, hbm_cap=150e9, max_active=args.max_active)
+    srv = serve.SolveServer(device, hbm_cap=150e9, max_active=args.max_active,
+                            max_queue_s=args.serve_max_queue)
     with ClockSampler(local) as clk:
         res = srv.run(reqs, realtime=True)
     st = dict(srv.stats)
     wall = max_over_ranks(st['wall_s'], world)
     barrier(world)
-    seq, t_seq = serve.run_sequential(reqs, device)
+    # sequential baseline: the served requests (or a seeded sample of them),
+    # each solved alone with the same stopping rules
+    served_ids = [r.rid for r in res if not r.shed]
+    if args.serve_seq_sample and args.serve_seq_sample < len(served_ids):
+        rng = np.random.default_rng(11 + rank)
+        served_ids = sorted(rng.choice(served_ids, args.serve_seq_sample, replace=False).tolist())
+    by_id = {r.rid: r for r in reqs}
+    sample = [by_id[i] for i in served_ids]
+    seq, t_seq, t_seq_wall = serve.run_sequential(sample, device, with_wall=True)
     t_seq = max_over_ranks(t_seq, world)
-    same = all((a.steps, a.converged) == (b.steps, b.converged)
-               for a, b in zip(sorted(res, key=lambda r: r.rid), seq))
+    t_seq_wall = max_over_ranks(t_seq_wall, world)
+    res_by_id = {r.rid: r for r in res}
+    same = all((res_by_id[b.rid].steps, res_by_id[b.rid].converged) == (b.steps, b.converged)
+               for b in seq)
+    seq_gps = sum(b.steps * b.grid_points for b in seq)
     gps = st['grid_point_steps']
     kinds = {}
     for r in res:
+        if r.shed:
+            continue
         k = kinds.setdefault(f'{r.kind}_{int(round(r.grid_points ** 0.5))}',
                              {'n': 0, 'steps': 0, 'converged': 0, 'lat': []})
         k['n'] += 1
@@ -604,18 +701,24 @@ def run_served(args, world, rank, local):
                     'grid_point_steps_per_s_upper_bound':
                         offered_max / args.serve_window},
         'served': {'grid_point_steps': gps, 'wall_s': wall,
-                   'requests_per_s': len(res) / wall,
+                   'requests_served': st['served'], 'requests_shed': st['shed'],
+                   'max_queue_s': args.serve_max_queue,
+                   'requests_per_s': st['served'] / wall,
                    'peak_active': st['peak_active'],
                    'peak_admitted_bytes': st['peak_admitted_bytes'],
                    'by_kind': kinds},
-        'sequential_plain': {'value': world * gps / t_seq,
+        'sequential_plain': {'value': world * seq_gps / t_seq,
                              'unit': 'grid-point-steps/s',
-                             'device_s': t_seq,
-                             'what': 'the same requests with the same stopping '
-                                     'rules, each solved alone by the plain '
-                                     'drop-in (device time of the stepping; '
-                                     'host set-up excluded)'},
-        'speedup_vs_sequential': t_seq / wall,
+                             'device_s': t_seq, 'requests': len(seq),
+                             'with_host_setup': {'value': world * seq_gps / t_seq_wall,
+                                                 'wall_s': t_seq_wall},
+                             'what': 'served requests (all, or a seeded sample) with '
+                                     'the same stopping rules, each solved alone by '
+                                     'the plain drop-in: device time of the stepping '
+                                     '(host set-up excluded), and host wall time '
+                                     'including each set-up'},
+        'speedup_vs_sequential': (gps / wall) / (seq_gps / t_seq),
+        'speedup_vs_sequential_with_setup': (gps / wall) / (seq_gps / t_seq_wall),
         'same_steps_alone_and_in_mix': same,
         'clocks': clk.summary(),
     }

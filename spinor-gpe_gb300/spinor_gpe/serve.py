@@ -21,6 +21,11 @@ Stopping rules
     when |E(n) - E(n-1)| < tol, or at ``max_steps``.
   * no ``tol`` (real time): the solve runs ``max_steps`` steps.
 
+Load shedding: with ``max_queue_s`` a request that has waited longer than
+that for admission is rejected (reported with ``shed=True`` and no steps)
+instead of joining an ever longer queue, so an overloaded stream keeps a
+bounded latency for the requests it serves.
+
 Host set-up (building a propagator: FP64 operators on the host, plan
 creation and uploads) runs on a helper thread, so the loop that feeds the GPU
 never waits on it.  Freeing device memory synchronises the device, so a
@@ -73,6 +78,7 @@ class SolveResult:
     finished: float
     grid_points: int
     psik: Optional[list] = None
+    shed: bool = False
 
     @property
     def latency(self):
@@ -148,12 +154,16 @@ class SolveServer:
     ``hbm_cap``: device bytes the admitted solves may hold together;
     ``max_active``: solves admitted at once (one CUDA stream each);
     ``keep_psik``: return each final k-space spinor (device tensors);
-    ``build_workers``: helper threads building admitted solves.
+    ``build_workers``: helper threads building admitted solves;
+    ``max_queue_s``: shed requests that waited longer than this for admission
+    (None: never shed).
     """
 
     def __init__(self, device='cuda', hbm_cap=150e9, max_active=64,
-                 keep_psik=False, build_workers=4, clock=time.perf_counter):
+                 keep_psik=False, build_workers=4, clock=time.perf_counter,
+                 max_queue_s=None):
         self.device = torch.device(device)
+        self.max_queue_s = None if max_queue_s is None else float(max_queue_s)
         self.hbm_cap = float(hbm_cap)
         self.max_active = int(max_active)
         self.keep_psik = keep_psik
@@ -209,6 +219,12 @@ class SolveServer:
             now = self.clock() - t0
             while arrivals and (not realtime or arrivals[0].arrival <= now):
                 pending.append(arrivals.popleft())
+            if self.max_queue_s is not None:
+                while pending and now - pending[0].arrival > self.max_queue_s:
+                    req = pending.popleft()
+                    results[req.rid] = SolveResult(
+                        req.rid, req.kind, 0, False, None, None, req.arrival,
+                        now, now, req.grid_points, None, shed=True)
             # admission: first come, first served, under slots and memory
             if (pending and free_streams and parked
                     and used + parked_bytes + pending[0].footprint > self.hbm_cap):
@@ -266,9 +282,11 @@ class SolveServer:
         pool.shutdown(wait=True)
         self._release(parked)
         res = [results[r.rid] for r in requests]
-        lat = np.array([r.latency for r in res]) if res else np.zeros(1)
+        done = [r for r in res if not r.shed]
+        lat = np.array([r.latency for r in done]) if done else np.zeros(1)
         gps = sum(r.steps * r.grid_points for r in res)
-        self.stats = {'requests': len(res), 'wall_s': wall,
+        self.stats = {'requests': len(res), 'served': len(done),
+                      'shed': len(res) - len(done), 'wall_s': wall,
                       'grid_point_steps': gps,
                       'grid_point_steps_per_s': gps / wall if wall > 0 else 0.0,
                       'p50_ms': float(np.percentile(lat, 50) * 1e3),
@@ -279,10 +297,11 @@ class SolveServer:
         return res
 
 
-def run_sequential(requests, device='cuda'):
+def run_sequential(requests, device='cuda', with_wall=False):
     """The same requests solved one after another with the plain propagator
     and the same stopping rules, on the current stream.  Returns the results
-    and the device time of the stepping (set-up excluded), in seconds."""
+    and the device time of the stepping (set-up excluded), in seconds; with
+    ``with_wall`` also the host wall time including each request's set-up."""
     device = torch.device(device)
     if device.index is None:
         device = torch.device('cuda', torch.cuda.current_device())
@@ -290,6 +309,7 @@ def run_sequential(requests, device='cuda'):
     stream = torch.cuda.current_stream(device)
     total = 0.0
     out = []
+    t_wall = time.perf_counter()
     for req in sorted(requests, key=lambda r: (r.arrival, r.rid)):
         prop = req.make()
         torch.cuda.synchronize(device)
@@ -309,6 +329,9 @@ def run_sequential(requests, device='cuda'):
                                s.energy, s.d_energy, req.arrival, 0.0, 0.0,
                                req.grid_points))
         del s, prop
+    torch.cuda.synchronize(device)
+    if with_wall:
+        return out, total, time.perf_counter() - t_wall
     return out, total
 
 

@@ -118,3 +118,26 @@ def test_served_requests_with_device_set_up(tmp_path):
     res = serve.SolveServer(max_active=4).run(reqs, realtime=False)
     assert len(res) == len(reqs) and all(r.steps > 0 for r in res)
     assert all(np.isfinite(r.energy) for r in res)
+
+
+@pytest.mark.gpu
+def test_requests_past_the_queue_limit_are_shed(tmp_path):
+    """With one slot and a queue-time limit shorter than one request's
+    set-up, the requests behind the first are shed (no steps, flagged), and
+    the one served matches the same request served alone."""
+    import time as _time
+    reqs = _small_requests(tmp_path)
+    slow = []
+    for r in reqs:
+        def make(m=r.make):
+            _time.sleep(0.3)             # a set-up longer than the queue limit
+            return m()
+        slow.append(serve.SolveRequest(r.rid, 0.0, make, r.footprint, r.max_steps,
+                                       r.tol, r.chunk, r.grid_points, r.kind))
+    srv = serve.SolveServer(max_active=1, max_queue_s=0.1)
+    res = srv.run(slow, realtime=True)
+    assert srv.stats['served'] == 1 and srv.stats['shed'] == len(slow) - 1
+    assert not res[0].shed and res[0].steps > 0
+    assert all(r.shed and r.steps == 0 for r in res[1:])
+    alone = serve.SolveServer(max_active=1).run([reqs[0]])[0]
+    assert (alone.steps, alone.energy) == (res[0].steps, res[0].energy)

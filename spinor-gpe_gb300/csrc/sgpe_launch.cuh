@@ -119,24 +119,16 @@ constexpr int kMaxShapes = 3;
 constexpr bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 template <typename R> struct ShapeTune;
 template <> struct ShapeTune<float> {
-  // rows: 8 / 4 points per thread up to 512; at 1024 two alternatives, 32
-  // points per thread (two radix-32 stages, warp-synchronous lines, 128
-  // registers) and 8 (four stages, 256-thread rows, more warps per SM for
-  // the many-wave launches of grouped batches); sides 3 * 2^k: the other
-  // multiple of 3 (12 <-> 24)
+  // rows: 8 / 4 points per thread up to 512; at 1024 one alternative with
+  // 32 points per thread (two radix-32 stages, warp-synchronous lines,
+  // 128 registers); sides 3 * 2^k: the other multiple of 3 (12 <-> 24)
   static constexpr int r3_alt(int n) { return n >= 768 ? 12 : 24; }
   static constexpr int row_shapes(int n) {
-    return n % 3 == 0 ? 2 : !is_pow2(n) ? 1 : n <= 512 ? 3 : n == 1024 ? 3 : 1;
+    return n % 3 == 0 ? 2 : !is_pow2(n) ? 1 : n <= 512 ? 3 : n == 1024 ? 2 : 1;
   }
-  // columns: 8 points per thread up to 1024 (shape 1; shape 2 with 4-column
-  // tiles up to 512)
-  static constexpr int col_shapes(int n) {
-    return n % 3 == 0 ? 2 : (is_pow2(n) && n <= 512) ? 3 : n == 1024 ? 2 : 1;
-  }
-  static constexpr int row_e(int n, int s) {
-    return n % 3 == 0 ? r3_alt(n) : n == 1024 ? (s == 1 ? 32 : 8) : s == 1 ? 8 : 4;
-  }
-  static constexpr int row_minb(int n, int s) { return (n == 1024 && s == 1) ? 4 : 0; }  // 0: the shape-0 rule
+  static constexpr int col_shapes(int n) { return n % 3 == 0 ? 2 : (is_pow2(n) && n <= 512) ? 3 : 1; }
+  static constexpr int row_e(int n, int s) { return n % 3 == 0 ? r3_alt(n) : n == 1024 ? 32 : s == 1 ? 8 : 4; }
+  static constexpr int row_minb(int n, int) { return n == 1024 ? 4 : 0; }  // 0: the shape-0 rule
   static constexpr int row_threads(int, int) { return Tune<float>::ROW_THREADS; }
   static constexpr int col_e(int n, int) { return n % 3 == 0 ? r3_alt(n) : 8; }
   static constexpr int cols(int n, int s) { return (n % 3 != 0 && s == 2) ? 4 : Tune<float>::COLS; }

@@ -34,8 +34,8 @@ def test_shape_counts(native_lib):
     lib = _native.load()
     assert lib.sgpe_shape_count(64, 0, 512) == 3
     assert lib.sgpe_shape_count(64, 1, 32) == 3
-    assert lib.sgpe_shape_count(64, 0, 1024) == 3
-    assert lib.sgpe_shape_count(64, 1, 1024) == 2
+    assert lib.sgpe_shape_count(64, 0, 1024) == 2
+    assert lib.sgpe_shape_count(64, 1, 1024) == 1
     assert lib.sgpe_shape_count(48, 0, 1024) == 1          # double-float: shape 0
     assert lib.sgpe_shape_count(48, 1, 192) == 1
     assert lib.sgpe_shape_count(64, 0, 2048) == 1
@@ -181,8 +181,8 @@ def test_radix3_sides_every_shape(tp, tmp_path, n):
 
 @pytest.mark.gpu
 def test_raman_1024_complex64_every_shape(tp, tmp_path):
-    """1024^2 complex64: every pair of the row shapes (16, 32 and 8 points
-    per thread) and column shapes (16 and 8) against the oracle."""
+    """1024^2 complex64: both row shapes (16 and 32 points per thread)
+    against the oracle."""
     from spinor_gpe import workloads
     from spinor_gpe.pspinor import pspinor as spin
     from spinor_gpe.pspinor import tensor_tools as ttools
@@ -191,7 +191,7 @@ def test_raman_1024_complex64_every_shape(tp, tmp_path):
     n = 3
     ref = _oracle(ps, 1e-3, 'real', n)
     pairs = _pairs(64, 1024, 1024)
-    assert len(pairs) == 6
+    assert len(pairs) == 2
     for shapes in pairs:
         prop = tp.TensorPropagator(ps, 1e-3, n, 'cuda', time='real', dtype=64, kernel_shapes=shapes)
         prop.full_steps(n)

@@ -95,6 +95,28 @@ template <class C> __device__ __forceinline__ C cmul(C a, C b) {
 template <class C> __device__ __forceinline__ C cmulc(C a, C b) {
   return cmake<C>(fmadd(a.x, b.x, a.y * b.y), fmadd(a.y, b.x, -a.x * b.y));
 }
+// Double-float butterflies: sums without renormalisation (df_add_lazy),
+// each value renormalised once at the end of its transform stage
+// (fft_stage).  (1) on, (0) renormalise every sum.
+#ifndef SGPE_DF_LAZY
+#define SGPE_DF_LAZY 1
+#endif
+#if SGPE_DF_LAZY
+template <> __device__ __forceinline__ DFC cadd<DFC>(DFC a, DFC b) {
+  return DFC{df_add_lazy(a.x, b.x), df_add_lazy(a.y, b.y)};
+}
+template <> __device__ __forceinline__ DFC csub<DFC>(DFC a, DFC b) {
+  return DFC{df_add_lazy(a.x, -b.x), df_add_lazy(a.y, -b.y)};
+}
+#endif
+template <class C> __device__ __forceinline__ void renorm(C&) {}
+template <> __device__ __forceinline__ void renorm<DFC>(DFC& a) {
+  if (SGPE_DF_LAZY) {
+    a.x = df_renorm(a.x);
+    a.y = df_renorm(a.y);
+  }
+}
+
 // double-float complex products: each part one two-product dot (df_dot2)
 template <> __device__ __forceinline__ DFC cmul<DFC>(DFC a, DFC b) {
   return DFC{df_dot2<-1>(a.x, b.x, a.y, b.y), df_dot2<1>(a.x, b.y, a.y, b.x)};
@@ -590,6 +612,8 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
     for (int q = 0; q < Q; ++q) {
       if constexpr (SM::kTc && R == 16) tc_dft16<DIR>(a[l][q], sm.tc);
       else Dft<R, DIR>::run(a[l][q]);
+#pragma unroll
+      for (int r = 0; r < R; ++r) renorm(a[l][q][r]);
     }
   if constexpr (kLast && !TO_SMEM) {
 #pragma unroll

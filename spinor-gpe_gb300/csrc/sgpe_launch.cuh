@@ -65,6 +65,7 @@ template <> struct Tune<float> {
   static constexpr int COL_E = SGPE_F32_COL_E, COLS = SGPE_F32_COLS, COL_MINB = SGPE_F32_COL_MINB;
   static constexpr int R3_E = SGPE_F32_R3_E, R3_ROW_MINB = SGPE_F32_R3_ROW_MINB, R3_COL_MINB = SGPE_F32_R3_COL_MINB;
   static constexpr int R3_E_LARGE = SGPE_F32_R3_E_LARGE, R3_COL_MINB_LARGE = SGPE_F32_R3_COL_MINB_LARGE;
+  static constexpr int COL_MAX_THREADS = 1024;
 };
 template <> struct Tune<double> {
   static constexpr int ROW_E = 8, ROW_THREADS = 256, ROW_MINB = 2;
@@ -72,6 +73,7 @@ template <> struct Tune<double> {
   static constexpr int COL_E = 8, COLS = 4, COL_MINB = 1;
   static constexpr int R3_E = 12, R3_ROW_MINB = 2, R3_COL_MINB = 1;
   static constexpr int R3_E_LARGE = 12, R3_COL_MINB_LARGE = 1;
+  static constexpr int COL_MAX_THREADS = 1024;
 };
 // Double-float: a complex value is four FP32 registers, so 8 points per
 // thread (12 for sides 3 * 2^k), 128-register caps (two 256-thread blocks
@@ -88,12 +90,15 @@ template <> struct Tune<double> {
 #ifndef SGPE_DF_COL_MINB
 #define SGPE_DF_COL_MINB 1
 #endif
+// Sides of 2048 and more: one 512-thread block per SM for rows and at most
+// 512-thread column blocks, so that the 128-register cap holds (no spills).
 template <> struct Tune<DF> {
   static constexpr int ROW_E = 8, ROW_THREADS = SGPE_DF_ROW_THREADS, ROW_MINB = SGPE_DF_ROW_MINB;
-  static constexpr int ROW_E_LARGE = 8, ROW_MINB_LARGE = SGPE_DF_ROW_MINB;
+  static constexpr int ROW_E_LARGE = 8, ROW_MINB_LARGE = 1;
   static constexpr int COL_E = 8, COLS = SGPE_DF_COLS, COL_MINB = SGPE_DF_COL_MINB;
   static constexpr int R3_E = 12, R3_ROW_MINB = SGPE_DF_ROW_MINB, R3_COL_MINB = SGPE_DF_COL_MINB;
   static constexpr int R3_E_LARGE = 12, R3_COL_MINB_LARGE = SGPE_DF_COL_MINB;
+  static constexpr int COL_MAX_THREADS = 512;
 };
 
 constexpr int cmin(int a, int b) { return a < b ? a : b; }
@@ -179,7 +184,8 @@ template <typename R, int N, int S = 0> struct ColCfg {
   static constexpr bool VALID = S < col_shape_count<R>(N);
   static constexpr int E = S == 0 ? pick_e<R>(N, Tune<R>::COL_E) : cmin(N, ShapeTune<R>::col_e(N, S));
   static constexpr int T = N / E;
-  static constexpr int COLS = cmax(cmin(S == 0 ? Tune<R>::COLS : ShapeTune<R>::cols(N, S), 1024 / T), 32 / T);
+  static constexpr int COLS =
+      cmax(cmin(S == 0 ? Tune<R>::COLS : ShapeTune<R>::cols(N, S), Tune<R>::COL_MAX_THREADS / T), 32 / T);
   static constexpr int THREADS = T * COLS;
   static constexpr size_t SMEM = size_t(COLS) * (N + N / E + 2) * sizeof(Cx<R>);
   static constexpr int MINB = cmax(

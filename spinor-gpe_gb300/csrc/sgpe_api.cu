@@ -136,6 +136,8 @@ struct sgpe_plan {
   void* s[2] = {nullptr, nullptr};
   void* scratch[2] = {nullptr, nullptr};
   double* part = nullptr;    // column-pass partial sums [2][ntile][2]
+  double* fin = nullptr;     // their sums (3 doubles) and the pass's arrival
+  unsigned* count = nullptr; // counter, behind the partials in `part`
   int ntile = 0;             // column tiles of the current kernels
   int ntile_fp32 = 0;        // ... of the FP32 DFT kernels
   int tc = 0;                // radix-16 stages on the tensor cores (split-BF16)
@@ -590,6 +592,8 @@ template <typename R> bool col_step_args(sgpe_plan* p, int sub, bool want_u, sgp
   }
   a.scale = R(1);
   a.part = reinterpret_cast<R*>(p->part);
+  a.fin = p->fin;
+  a.count = p->count;
   return true;
 }
 
@@ -615,6 +619,7 @@ template <typename R> sgpe::RowArgs<R> row_step_args(sgpe_plan* p, int sub, doub
   a.scale = R(1);
   a.part = reinterpret_cast<R*>(p->part);
   a.ntile = p->ntile;
+  a.fin = p->fin;
   a.norm_num = p->atom_num / (double(p->nx) * double(p->ny) * p->dv_r);
   a.g_uu = R(p->g[0]);
   a.g_dd = R(p->g[1]);
@@ -1122,9 +1127,13 @@ int sgpe_plan_create(sgpe_plan** out, int ny, int nx, int dtype_bits, int device
   cudaError_t e = cudaSuccess;
   for (int c = 0; c < 2 && e == cudaSuccess; ++c) e = cudaMalloc(&p->s[c], p->elem * (size_t)nx * ny);
   // room for one tile per column: every kernel configuration fits
-  const size_t red_bytes = sizeof(double) * 4 * (size_t)nx;
+  const size_t red_bytes = sizeof(double) * 4 * (size_t)nx + 64;  // + final sums and counter
   if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&p->part), red_bytes);
   if (e == cudaSuccess) e = cudaMemset(p->part, 0, red_bytes);
+  if (e == cudaSuccess) {
+    p->fin = p->part + 4 * (size_t)nx;
+    p->count = reinterpret_cast<unsigned*>(p->fin + 4);
+  }
   if (e == cudaSuccess) {
     by_prec(dtype_bits, [&](auto t) {
       using R = decltype(t);

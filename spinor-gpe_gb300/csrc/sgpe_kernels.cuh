@@ -214,6 +214,10 @@ template <typename R> struct RowArgs {
   // column pass, lambda = sqrt(norm_num / sum w)
   const R* part;          // [2 comps][ntile][u, w]
   int ntile;
+  // non-null: the sums of those partials (sum u_0, sum u_1, sum w), formed
+  // once by the last block of the column pass (ColArgs::fin); read instead
+  // of summing the partials in every block
+  const double* fin;
   double norm_num;        // atom_num / (Nx Ny dv_r)
   R g_uu, g_dd, g_ud;
   int coupling;
@@ -241,6 +245,11 @@ template <typename R> struct ColArgs {
   R* part;                // non-null: per-block partial sums [comp][tile][u, w]
                           // in the working precision; the consumer of the
                           // pass sums them with (at least) FP64 accuracy
+  // non-null (with part): the block that finishes last sums the partials
+  // (sum_partials, the order every consumer uses) into fin[0..2] and resets
+  // the arrival counter *count to zero for the next pass
+  double* fin;
+  unsigned* count;
   int tc;                 // launch the tensor-core DFT16 kernels (host side)
   const uint32_t* tcb;    // their B fragments (kTcBfragWords, device)
   int shape;              // kernel shape of the launch (host side)
@@ -403,6 +412,25 @@ __device__ __forceinline__ DF row_lambda(const DF* part, int ntile, int lane, DF
     *u1 = from_df(b);
   }
   return to_df(sqrt(from_df(norm_num) / from_df(c)));
+}
+
+// lambda (and the population sums) from the column pass's final sums
+// (u0, u1, w) as exact FP64 values of the sums above: the same bits as
+// row_lambda computes from the partials.
+__device__ __forceinline__ float row_lambda_final(const double* f, float norm_num, double* u0, double* u1) {
+  *u0 = f[0];
+  *u1 = f[1];
+  return sqrtf(norm_num / float(f[2]));
+}
+__device__ __forceinline__ double row_lambda_final(const double* f, double norm_num, double* u0, double* u1) {
+  *u0 = f[0];
+  *u1 = f[1];
+  return sqrt(norm_num / f[2]);
+}
+__device__ __forceinline__ DF row_lambda_final(const double* f, DF norm_num, double* u0, double* u1) {
+  *u0 = f[0];
+  *u1 = f[1];
+  return to_df(sqrt(from_df(norm_num) / f[2]));
 }
 
 // Sum of |v[m]|^2 over the E points of a thread, pairwise in the working
@@ -693,7 +721,8 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
     if (tid < 32) {
       double su0 = 0.0, su1 = 0.0;
       const bool want_u = (a.pops != nullptr && blockIdx.x == 0);
-      const R l = row_lambda(a.part, a.ntile, tid, R(a.norm_num), &su0, &su1, want_u);
+      const R l = a.fin != nullptr ? row_lambda_final(a.fin, R(a.norm_num), &su0, &su1)
+                                   : row_lambda(a.part, a.ntile, tid, R(a.norm_num), &su0, &su1, want_u);
       if (tid == 0) {
         s_lambda = l;
         if (want_u) {
@@ -936,6 +965,27 @@ __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
         R* dst = a.part + 2 * ((long long)comp * gridDim.x + blockIdx.x);
         dst[0] = bu;
         dst[1] = bw;
+      }
+    }
+    if (a.fin != nullptr) {
+      // the last block to finish sums every block's partials (no block waits)
+      __shared__ bool s_last;
+      if (tid == 0) {
+        __threadfence();  // this block's partial is visible before its arrival
+        const unsigned ticket = atomicAdd(a.count, 1u);
+        s_last = (ticket == gridDim.x * gridDim.y - 1);
+      }
+      __syncthreads();
+      if (s_last && warp == 0) {
+        __threadfence();
+        double su0, su1, sw;
+        sum_partials(static_cast<const R*>(a.part), int(gridDim.x), lane, &su0, &su1, &sw);
+        if (lane == 0) {
+          a.fin[0] = su0;
+          a.fin[1] = su1;
+          a.fin[2] = sw;
+          *a.count = 0u;
+        }
       }
     }
   }

@@ -138,6 +138,12 @@ struct sgpe_plan {
   double* part = nullptr;    // column-pass partial sums [2][ntile][2]
   double* fin = nullptr;     // their sums (3 doubles) and the pass's arrival
   unsigned* count = nullptr; // counter, behind the partials in `part`
+  // the last column block forms the sums once and row blocks read them
+  // (double-float plans, where every row block re-summing the partials in
+  // double-float arithmetic cost ~10% of the row pass); complex64 and
+  // complex128 row blocks sum the partials themselves while their other
+  // warps transform, which costs less than a serial tail on the column pass
+  bool final_sums = false;
   int ntile = 0;             // column tiles of the current kernels
   int ntile_fp32 = 0;        // ... of the FP32 DFT kernels
   int tc = 0;                // radix-16 stages on the tensor cores (split-BF16)
@@ -592,7 +598,7 @@ template <typename R> bool col_step_args(sgpe_plan* p, int sub, bool want_u, sgp
   }
   a.scale = R(1);
   a.part = reinterpret_cast<R*>(p->part);
-  a.fin = p->fin;
+  a.fin = p->final_sums ? p->fin : nullptr;
   a.count = p->count;
   return true;
 }
@@ -619,7 +625,7 @@ template <typename R> sgpe::RowArgs<R> row_step_args(sgpe_plan* p, int sub, doub
   a.scale = R(1);
   a.part = reinterpret_cast<R*>(p->part);
   a.ntile = p->ntile;
-  a.fin = p->fin;
+  a.fin = p->final_sums ? p->fin : nullptr;
   a.norm_num = p->atom_num / (double(p->nx) * double(p->ny) * p->dv_r);
   a.g_uu = R(p->g[0]);
   a.g_dd = R(p->g[1]);
@@ -1110,6 +1116,9 @@ int sgpe_plan_create(sgpe_plan** out, int ny, int nx, int dtype_bits, int device
   // SGPE_DISABLE_GRAPHS (any value) makes this plan launch every step
   // eagerly; used to check graph replay against eager launches.
   p->graphs_enabled = std::getenv("SGPE_DISABLE_GRAPHS") == nullptr;
+  // SGPE_FINAL_SUMS=0/1 overrides the precision's choice (measurements)
+  const char* fs = std::getenv("SGPE_FINAL_SUMS");
+  p->final_sums = fs != nullptr ? fs[0] == '1' : dtype_bits == SGPE_DTYPE_DF;
   p->row_shape = default_shape(dtype_bits, 0, nx);
   p->col_shape = default_shape(dtype_bits, 1, ny);
   int cols = by_prec(dtype_bits, [&](auto t) { return sgpe::col_tile_width<decltype(t)>(ny, p->col_shape); });

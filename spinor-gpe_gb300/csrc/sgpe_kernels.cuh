@@ -433,6 +433,47 @@ __device__ __forceinline__ DF row_lambda_final(const double* f, DF norm_num, dou
   return to_df(sqrt(from_df(norm_num) / f[2]));
 }
 
+// Sums (u_0, u_1, w) of the column-pass partials [2][ntile][u, w] by every
+// thread of one block, in FP64 (the partials' values are exact in FP64):
+// each thread adds a strided share (all loads in flight at once), then warp
+// butterflies and warp 0 combine the warps in a fixed order.  Called by the
+// block that finishes a column pass last; out[0..2] receive the sums.
+template <typename R> __device__ __forceinline__ double partial_value(const R* p) { return double(*p); }
+template <> __device__ __forceinline__ double partial_value<DF>(const DF* p) { return from_df(*p); }
+template <typename R>
+__device__ __forceinline__ void final_sums(const R* part, int ntile, int tid, int nthreads, double* out) {
+  __shared__ double s_sum[3][32];
+  double u0 = 0.0, u1 = 0.0, w = 0.0;
+  for (int i = tid; i < 2 * ntile; i += nthreads) {
+    const double u = partial_value(part + 2 * i), ww = partial_value(part + 2 * i + 1);
+    w += ww;
+    if (i < ntile) u0 += u; else u1 += u;
+  }
+  u0 = warp_sum(u0);
+  u1 = warp_sum(u1);
+  w = warp_sum(w);
+  const int warp = tid >> 5, lane = tid & 31, nw = (nthreads + 31) >> 5;
+  if (lane == 0) {
+    s_sum[0][warp] = u0;
+    s_sum[1][warp] = u1;
+    s_sum[2][warp] = w;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    u0 = lane < nw ? s_sum[0][lane] : 0.0;
+    u1 = lane < nw ? s_sum[1][lane] : 0.0;
+    w = lane < nw ? s_sum[2][lane] : 0.0;
+    u0 = warp_sum(u0);
+    u1 = warp_sum(u1);
+    w = warp_sum(w);
+    if (lane == 0) {
+      out[0] = u0;
+      out[1] = u1;
+      out[2] = w;
+    }
+  }
+}
+
 // Sum of |v[m]|^2 over the E points of a thread, pairwise in the working
 // precision.  Block sums continue pairwise (warp butterfly, then across
 // warps), so a block partial carries about log2(block points) roundings; only
@@ -976,16 +1017,10 @@ __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
         s_last = (ticket == gridDim.x * gridDim.y - 1);
       }
       __syncthreads();
-      if (s_last && warp == 0) {
+      if (s_last) {
         __threadfence();
-        double su0, su1, sw;
-        sum_partials(static_cast<const R*>(a.part), int(gridDim.x), lane, &su0, &su1, &sw);
-        if (lane == 0) {
-          a.fin[0] = su0;
-          a.fin[1] = su1;
-          a.fin[2] = sw;
-          *a.count = 0u;
-        }
+        final_sums(static_cast<const R*>(a.part), int(gridDim.x), tid, NT, a.fin);
+        if (tid == 0) *a.count = 0u;
       }
     }
   }

@@ -174,3 +174,33 @@ def test_long_horizon_real_time_1024_every_precision(tp, tmp_path):
     print('long-horizon errors', errs)
     for dtype, e in errs.items():
         assert e <= LONG_BOUND[dtype], (dtype, e)
+
+
+def test_double_float_in_a_batch_matches_alone(tp, tmp_path):
+    """A batch mixing a double-float plan with complex64 and complex128
+    plans (the double-float plan runs as its own graph branch) gives every
+    solve exactly what it gives alone; double-float plans have one kernel
+    shape, so autotuning leaves them as they are."""
+    from spinor_gpe.batch import PropagatorBatch
+    names = ['imag_raman_64', 'real_raman_32', 'imag_plain_32']
+    dtypes = [DF, 64, 128]
+
+    def make(i):
+        case = CASES[names[i]]
+        p = case_params(case)
+        return tp.TensorPropagator(spin_from_case(case, tmp_path / f'b{i}'), p['dt'], 8,
+                                   'cuda', time=p['time'], dtype=dtypes[i])
+    alone = []
+    for i in range(3):
+        prop = make(i)
+        prop.full_steps(12)
+        alone.append(_state(prop))
+    props = [make(i) for i in range(3)]
+    assert props[0].kernel_shapes == (0, 0)
+    props[0].autotune()
+    assert props[0].kernel_shapes == (0, 0)
+    batch = PropagatorBatch(props)
+    batch.full_steps(12)
+    for i, prop in enumerate(props):
+        np.testing.assert_array_equal(_state(prop), alone[i])
+    batch.close()

@@ -287,13 +287,29 @@ template <typename T> __device__ __forceinline__ T warp_sum(T v) {
 // Sums of the column-pass partials [2][ntile][u, w] by one warp, in a fixed
 // order: (sum u_0, sum u_1, sum w) returned on every lane.
 // FP64 partials are summed in FP64.
+// The partials are read kPartialBatch at a time per lane (independent loads
+// in flight together, one memory latency per batch instead of one per
+// entry) and added in the same order as one at a time.
+constexpr int kPartialBatch = 8;
+
 __device__ __forceinline__ void sum_partials(const double* part, int ntile, int lane, double* u0, double* u1,
                                              double* w) {
   double su0 = 0.0, su1 = 0.0, sw = 0.0;
-  for (int i = lane; i < 2 * ntile; i += 32) {
-    const double u = part[2 * i], ww = part[2 * i + 1];
-    sw += ww;
-    if (i < ntile) su0 += u; else su1 += u;
+  const double2* p2 = reinterpret_cast<const double2*>(part);
+  for (int i0 = lane; i0 < 2 * ntile; i0 += 32 * kPartialBatch) {
+    double2 v[kPartialBatch];
+#pragma unroll
+    for (int k = 0; k < kPartialBatch; ++k) {
+      const int i = i0 + 32 * k;
+      v[k] = i < 2 * ntile ? p2[i] : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int k = 0; k < kPartialBatch; ++k) {
+      const int i = i0 + 32 * k;
+      if (i >= 2 * ntile) break;
+      sw += v[k].y;
+      if (i < ntile) su0 += v[k].x; else su1 += v[k].x;
+    }
   }
   *u0 = warp_sum(su0);
   *u1 = warp_sum(su1);
@@ -341,10 +357,21 @@ struct FloatFloat {
 __device__ __forceinline__ void sum_partials(const float* part, int ntile, int lane, FloatFloat* u0,
                                              FloatFloat* u1, FloatFloat* w) {
   FloatFloat su0, su1, sw;
-  for (int i = lane; i < 2 * ntile; i += 32) {
-    const float2 uw = reinterpret_cast<const float2*>(part)[i];
-    sw.add(uw.y);
-    if (i < ntile) su0.add(uw.x); else su1.add(uw.x);
+  const float2* p2 = reinterpret_cast<const float2*>(part);
+  for (int i0 = lane; i0 < 2 * ntile; i0 += 32 * kPartialBatch) {
+    float2 v[kPartialBatch];
+#pragma unroll
+    for (int k = 0; k < kPartialBatch; ++k) {
+      const int i = i0 + 32 * k;
+      v[k] = i < 2 * ntile ? p2[i] : make_float2(0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int k = 0; k < kPartialBatch; ++k) {
+      const int i = i0 + 32 * k;
+      if (i >= 2 * ntile) break;
+      sw.add(v[k].y);
+      if (i < ntile) su0.add(v[k].x); else su1.add(v[k].x);
+    }
   }
   su0.warp_reduce();
   su1.warp_reduce();
@@ -366,10 +393,21 @@ __device__ __forceinline__ void sum_partials(const float* part, int ntile, int l
 // order (every lane ends with the same bits, as above).
 __device__ __forceinline__ void sum_partials(const DF* part, int ntile, int lane, DF* u0, DF* u1, DF* w) {
   DF su0(0), su1(0), sw(0);
-  for (int i = lane; i < 2 * ntile; i += 32) {
-    const float4 uw = reinterpret_cast<const float4*>(part)[i];
-    sw += DF(uw.z, uw.w);
-    if (i < ntile) su0 += DF(uw.x, uw.y); else su1 += DF(uw.x, uw.y);
+  const float4* p4 = reinterpret_cast<const float4*>(part);
+  for (int i0 = lane; i0 < 2 * ntile; i0 += 32 * kPartialBatch) {
+    float4 v[kPartialBatch];
+#pragma unroll
+    for (int k = 0; k < kPartialBatch; ++k) {
+      const int i = i0 + 32 * k;
+      v[k] = i < 2 * ntile ? p4[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int k = 0; k < kPartialBatch; ++k) {
+      const int i = i0 + 32 * k;
+      if (i >= 2 * ntile) break;
+      sw += DF(v[k].z, v[k].w);
+      if (i < ntile) su0 += DF(v[k].x, v[k].y); else su1 += DF(v[k].x, v[k].y);
+    }
   }
   *u0 = warp_sum(su0);
   *u1 = warp_sum(su1);

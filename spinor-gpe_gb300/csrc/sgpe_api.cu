@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <complex>
 #include <cstring>
 #include <string>
 #include <type_traits>
@@ -62,6 +63,12 @@ struct SepOps {
   bool kin = false, kin_real = false;
   DevField px[2], py[2], s01x, s10x;
   bool pot = false, cpl = false;
+  // coupling, potential and coupling as one 2x2 matrix per point:
+  // C P C = pb(y) A(x), A = C diag(pa_0, kappa pa_1) C an x-table per entry,
+  // when the potential's y factors of the components differ by a constant
+  // (pb_1 = kappa pb_0); built in FP64, rounded once
+  DevField m[4], mb;
+  bool fused = false, mb_real = false;
 };
 
 // True when every value of the field has a zero imaginary part.
@@ -457,6 +464,56 @@ int build_sep_kin(sgpe_plan* p, const HostField (&a)[2], const HostField (&b)[2]
   return SGPE_OK;
 }
 
+// The fused real-space tables of SepOps (coupling, potential, coupling):
+// with c the uniform coupling diagonal, s01/s10 the off-diagonal x-tables,
+// pa_c/pb_c the potential's x and y factors and pb_1(y) = kappa pb_0(y)
+// (checked to 1e-14 over every y), C diag(pa_0 pb_0, pa_1 pb_1) C =
+// pb_0(y) A(x) with
+//   A00 = c^2 d0 + s01 s10 d1,  A01 = c s01 (d0 + d1),
+//   A10 = c s10 (d0 + d1),      A11 = s10 s01 d0 + c^2 d1,
+// d0 = pa_0(x), d1 = kappa pa_1(x), all in FP64.  Leaves fused = false when
+// the y factors are not proportional.
+int build_fused(sgpe_plan* p, const HostField (&px)[2], const HostField (&py)[2], const HostField& s01,
+                const HostField& s10, double cr, double ci, SepOps* so, std::vector<void*>* allocs) {
+  typedef std::complex<double> cd;
+  const int nx = p->nx, ny = p->ny;
+  auto at = [](const HostField& f, int i) { return cd(f.v[2 * i], f.v[2 * i + 1]); };
+  const cd b00 = at(py[0], 0);
+  if (std::abs(b00) == 0.0) return SGPE_OK;
+  const cd kappa = at(py[1], 0) / b00;
+  for (int y = 0; y < ny; ++y) {
+    const cd b0 = at(py[0], y), b1 = at(py[1], y);
+    if (std::abs(b1 - kappa * b0) > 1e-14 * std::abs(b1) + 1e-300) return SGPE_OK;
+  }
+  const cd c(cr, ci);
+  HostField m[4], mb;
+  for (int k = 0; k < 4; ++k) {
+    m[k].sx = 1;
+    m[k].sy = 0;
+    m[k].v.assign(2 * (size_t)nx, 0.0);
+  }
+  for (int x = 0; x < nx; ++x) {
+    const cd d0 = at(px[0], x), d1 = kappa * at(px[1], x);
+    const cd a01 = at(s01, x), a10 = at(s10, x);
+    const cd v[4] = {c * c * d0 + a01 * a10 * d1, c * a01 * (d0 + d1), c * a10 * (d0 + d1),
+                     a10 * a01 * d0 + c * c * d1};
+    for (int k = 0; k < 4; ++k) {
+      m[k].v[2 * x] = v[k].real();
+      m[k].v[2 * x + 1] = v[k].imag();
+    }
+  }
+  mb = py[0];
+  for (int k = 0; k < 4; ++k) {
+    const int rc = upload_host_field(p, m[k], &so->m[k], allocs);
+    if (rc != SGPE_OK) return rc;
+  }
+  const int rc = upload_host_field(p, mb, &so->mb, allocs);
+  if (rc != SGPE_OK) return rc;
+  so->mb_real = imag_zero(mb);
+  so->fused = true;
+  return SGPE_OK;
+}
+
 constexpr int kEnergyBlocks = 304;
 
 // FP64 upload of a field (energy fields keep double precision).
@@ -538,6 +595,16 @@ template <typename R> sgpe::KinOp<R> kin_op(const SubOps& so) {
 
 template <typename R> sgpe::KinOp<R> kin_pair(const PairOps& po) { return kin_from<R>(po.a, po.b, po.sep, po.real); }
 
+// SGPE_FUSED_OPS=0 keeps coupling, potential and coupling as three
+// operators (measurements and checks); on by default.
+bool fused_ops_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("SGPE_FUSED_OPS");
+    return !(e != nullptr && e[0] == '0');
+  }();
+  return on;
+}
+
 template <typename R> sgpe::RealOp<R> real_op(const SubOps& so, int coupling) {
   sgpe::RealOp<R> o;
   const bool sep = so.sep.pot && (!coupling || so.sep.cpl);
@@ -552,6 +619,12 @@ template <typename R> sgpe::RealOp<R> real_op(const SubOps& so, int coupling) {
   o.s01 = typed<R>(sep && coupling ? so.sep.s01x : so.has_s01 ? so.s01 : so.cs);
   o.s10 = typed<R>(sep && coupling ? so.sep.s10x : so.has_s01 ? so.s10 : so.cs);
   o.sep = sep ? 1 : 0;
+  o.fused = (sep && coupling && so.sep.fused && fused_ops_enabled()) ? 1 : 0;
+  if (o.fused) {
+    for (int k = 0; k < 4; ++k) o.m[k] = typed<R>(so.sep.m[k]);
+    o.mb = typed<R>(so.sep.mb);
+    o.real_mb = so.sep.mb_real ? 1 : 0;
+  }
   o.real_pot = so.pot_real ? 1 : 0;
   o.real_cc = so.cc_real ? 1 : 0;
   o.zr = R(so.zr);
@@ -1352,6 +1425,10 @@ int sgpe_set_substep(sgpe_plan* p, int sub, const sgpe_substep_ops* ops) {
       rc = upload_host_field(p, s01x, &so.sep.s01x, &so.allocs);
       if (rc == SGPE_OK) rc = upload_host_field(p, s10x, &so.sep.s10x, &so.allocs);
       so.sep.cpl = (rc == SGPE_OK);
+    }
+    if (rc == SGPE_OK && so.sep.pot && so.sep.cpl) {
+      const HostField hc = host_field(ops->cpl_c);
+      rc = build_fused(p, px, py, s01x, s10x, hc.v[0], hc.v[1], &so.sep, &so.allocs);
     }
     if (rc != SGPE_OK) {
       free_sub(so);

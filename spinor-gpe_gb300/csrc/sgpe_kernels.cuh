@@ -154,6 +154,11 @@ template <typename R> struct RealOp {
   // zero imaginary parts (imaginary time): real multiplies give the same bits
   int real_pot, real_cc;
   R zr, zi;
+  // fused (with sep and coupling): coupling, potential and coupling as
+  // pb(y) A(x), m[0..3] = A00, A01, A10, A11 x-tables of Nx values, mb the
+  // y-table of Ny values (real_mb: zero imaginary parts)
+  int fused, real_mb;
+  Field<R> m[4], mb;
 };
 
 // Field slots of RealOp in a fixed order (for the per-row hoisting below).
@@ -540,7 +545,16 @@ __device__ __forceinline__ double exp_r(double x) { return exp(x); }
 // 2e-9 (sin, relative) and 1.2e-10 (cos) there, under half an FP32 ulp.
 // Larger arguments use the library sincosf.
 __device__ __forceinline__ void sin_cos_phase(float x, float* s, float* c) {
-  if (fabsf(x) <= 0.78539816f) {
+  if (fabsf(x) <= 0.125f) {
+    // real-time phases of a stable step are this small: sin to x^5 and cos
+    // to x^6 (omitted terms below 1e-9 relative / 2e-12 absolute there)
+    const float x2 = x * x;
+    float ps = fmadd(x2, 1.0f / 120.0f, -1.0f / 6.0f);
+    *s = fmadd(ps * x2, x, x);
+    float pc = fmadd(x2, -1.0f / 720.0f, 1.0f / 24.0f);
+    pc = fmadd(pc, x2, -0.5f);
+    *c = fmadd(pc, x2, 1.0f);
+  } else if (fabsf(x) <= 0.78539816f) {
     const float x2 = x * x;
     float ps = fmadd(x2, 1.0f / 362880.0f, -1.0f / 5040.0f);
     ps = fmadd(ps, x2, 1.0f / 120.0f);
@@ -629,6 +643,41 @@ __device__ __forceinline__ void apply_real_ops(Cx<R>& p0, Cx<R>& p1, const Point
   } else {
     p0 = cmul(p0, i0);
     p1 = cmul(p1, i1);
+  }
+}
+
+// The same with coupling, potential and coupling applied as one 2x2 matrix
+// per point, pb(y) A(x) (RealOp::fused): interaction, A, then pb times the
+// interaction again (pb is a scalar for both components, so it commutes).
+template <typename R>
+__device__ __forceinline__ void apply_fused_ops(Cx<R>& p0, Cx<R>& p1, const Cx<R> (&m)[4], Cx<R> pb,
+                                                const RowArgs<R>& a) {
+  using C = Cx<R>;
+  const RealOp<R>& op = a.op;
+  const R n0 = cabs2(p0), n1 = cabs2(p1);
+  const R e0 = fmadd(a.g_uu, n0, a.g_ud * n1);
+  const R e1 = fmadd(a.g_dd, n1, a.g_ud * n0);
+  const C i0 = cexp_z(op.zr, op.zi, e0);
+  const C i1 = cexp_z(op.zr, op.zi, e1);
+  const bool ireal = (op.zi == R(0));
+  if (ireal) {
+    p0 = cscale(p0, i0.x);
+    p1 = cscale(p1, i1.x);
+  } else {
+    p0 = cmul(p0, i0);
+    p1 = cmul(p1, i1);
+  }
+  const C q0 = cadd(cmul(m[0], p0), cmul(m[1], p1));
+  const C q1 = cadd(cmul(m[2], p0), cmul(m[3], p1));
+  if (ireal && op.real_mb) {
+    p0 = cscale(q0, i0.x * pb.x);
+    p1 = cscale(q1, i1.x * pb.x);
+  } else if (ireal) {
+    p0 = cmul(q0, cscale(pb, i0.x));
+    p1 = cmul(q1, cscale(pb, i1.x));
+  } else {
+    p0 = cmul(q0, cmul(i0, pb));
+    p1 = cmul(q1, cmul(i1, pb));
   }
 }
 
@@ -827,6 +876,24 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
       auto at0 = [&](int m, int x) -> C& { return kOpsFold ? q0[m * kStep] : r0.line(0)[LS0::pad(unsigned(x))]; };
       auto at1 = [&](int m, int x) -> C& { return kOpsFold ? q1[m * kStep] : r1.line(0)[LS0::pad(unsigned(x))]; };
       if constexpr (SEP) {
+       if (a.coupling && a.op.fused) {
+        // coupling, potential, coupling as pb(y) A(x): four x-tables read at
+        // jj + m*2T, the row's pb hoisted
+        const C pb = ldg(a.op.mb.p + y);
+        const C* m0 = a.op.m[0].p + jj;
+        const C* m1 = a.op.m[1].p + jj;
+        const C* m2 = a.op.m[2].p + jj;
+        const C* m3 = a.op.m[3].p + jj;
+#pragma unroll ops_unroll<R>()
+        for (int m = 0; m < E / 2; ++m) {
+          const int x = jj + m * 2 * T;
+          C p0 = cscale(at0(m, x), lam), p1 = cscale(at1(m, x), lam);
+          const C mm[4] = {ldg(m0 + m * 2 * T), ldg(m1 + m * 2 * T), ldg(m2 + m * 2 * T), ldg(m3 + m * 2 * T)};
+          apply_fused_ops<R>(p0, p1, mm, pb, a);
+          at0(m, x) = p0;
+          at1(m, x) = p1;
+        }
+       } else {
         // separable operators: x-tables read at jj + m*2T (compile-time
         // offsets from one base), row values and the uniform c hoisted
         PointOps<R> v;
@@ -851,6 +918,7 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
           at0(m, x) = p0;
           at1(m, x) = p1;
         }
+       }
       } else {
         RowFields<R> rf;
         rf.init(a.op, y);

@@ -52,3 +52,17 @@ def test_argument_errors_without_gpu(native_lib):
     with pytest.raises(_native.SgpeError):
         _native.check(lib.sgpe_single_step(None, 0, None))
     assert lib.sgpe_version() >= 100
+
+
+def test_double_float_dtype_constant_and_parsing():
+    """The header's double-float dtype code is the one the binding passes;
+    the propagator accepts it by name and rejects other names before any
+    device work."""
+    m = re.search(r'#define\s+SGPE_DTYPE_DF\s+(\d+)', open(HEADER).read())
+    assert m and int(m.group(1)) == _native.SGPE_DTYPE_DF
+    from spinor_gpe.pspinor import tensor_propagator as tprop
+    for name in ('double-float', 'df', _native.SGPE_DTYPE_DF):
+        assert tprop._bits(name) == _native.SGPE_DTYPE_DF
+    assert tprop._bits('complex64') == 64 and tprop._bits(128) == 128
+    with pytest.raises(ValueError):
+        tprop._bits('bfloat16')

@@ -482,11 +482,8 @@ __host__ __device__ constexpr int tw_offset(int N, int E, int NS) {
 // bar > 0 (and !WARP): the line's threads are whole warps, and the
 // exchanges synchronise only them, on named barrier `bar` of `bar_threads`
 // threads, so lines of one block do not wait for each other.
-// TWS: the twiddle table passed to the transforms is a copy in shared memory
-// (plain loads instead of read-only global loads).
-template <class C, int E, bool WARP = false, bool TC = false, bool TWS = false> struct LineSmem {
+template <class C, int E, bool WARP = false, bool TC = false> struct LineSmem {
   static constexpr bool kTc = TC;
-  static constexpr bool kTwSmem = TWS;
   C* base;
   int line_stride;
   TcScratch tc;
@@ -506,9 +503,9 @@ template <class C, int E, bool WARP = false, bool TC = false, bool TWS = false> 
     }
   }
   // the same lines viewed as another complex type of the same size
-  template <class C2> __device__ __forceinline__ LineSmem<C2, E, WARP, TC, TWS> retype() const {
+  template <class C2> __device__ __forceinline__ LineSmem<C2, E, WARP, TC> retype() const {
     static_assert(sizeof(C2) == sizeof(C), "retyped lines must keep the element size");
-    return LineSmem<C2, E, WARP, TC, TWS>{reinterpret_cast<C2*>(base), line_stride, tc, bar, bar_threads};
+    return LineSmem<C2, E, WARP, TC>{reinterpret_cast<C2*>(base), line_stride, tc, bar, bar_threads};
   }
 };
 
@@ -585,7 +582,7 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
     static_assert(sizeof(TwE<decltype(C::x)>) == sizeof(C), "factorised twiddles need plain tables");
     C w1[R];
 #pragma unroll
-    for (int r = 1; r < R; ++r) w1[r] = SM::kTwSmem ? tw[kOff + j + (r - 1) * NS] : __ldg(tw + kOff + j + (r - 1) * NS);
+    for (int r = 1; r < R; ++r) w1[r] = __ldg(tw + kOff + j + (r - 1) * NS);
 #pragma unroll
     for (int q = 0; q < Q; ++q)
 #pragma unroll
@@ -603,7 +600,7 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
       const W* twq = reinterpret_cast<const W*>(tw) + kOff + (vt % NS);
 #pragma unroll
       for (int r = 1; r < R; ++r) {
-        const W w = SM::kTwSmem ? twq[(r - 1) * NS] : __ldg(twq + (r - 1) * NS);
+        const W w = __ldg(twq + (r - 1) * NS);
 #pragma unroll
         for (int l = 0; l < L; ++l) a[l][q][r] = tw_mul<DIR>(a[l][q][r], w);
       }

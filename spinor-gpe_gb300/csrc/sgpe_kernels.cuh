@@ -58,13 +58,6 @@
 #ifndef SGPE_COL_TMA_MIN_N
 #define SGPE_COL_TMA_MIN_N 512
 #endif
-// Column pass: each block copies the y transform's twiddle table into
-// shared memory once (two loads per thread at 1024) and its stages read it
-// there, instead of every thread issuing one read-only global load per
-// twiddle (the column pass's global-load queue is its busiest).
-#ifndef SGPE_COL_TW_SMEM
-#define SGPE_COL_TW_SMEM 1
-#endif
 
 // Unroll factor of the row kernel's point-wise loop (small: keeps the code
 // within the instruction cache).
@@ -989,14 +982,6 @@ row_kernel_grouped(const RowArgs<R>* __restrict__ args) {
 }
 
 // -------------------------------------------------------------- column pass
-// Bytes of a column block's exchange lines (16-byte aligned) and of the
-// twiddle copy behind them (SGPE_COL_TW_SMEM).
-template <typename R, int N, int E, int COLS> __host__ __device__ constexpr size_t col_exchange_bytes() {
-  return (sizeof(Cx<R>) * size_t(COLS) * (N + N / E + 2) + 15) & ~size_t(15);
-}
-template <typename R, int N, int E> __host__ __device__ constexpr size_t col_tw_bytes() {
-  return SGPE_COL_TW_SMEM ? sizeof(TwE<R>) * size_t(tw_offset(N, E, N) > 0 ? tw_offset(N, E, N) : 1) : 0;
-}
 template <typename R, int N, int E, int COLS, bool TC = false>
 __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
   using C = Cx<R>;
@@ -1072,18 +1057,8 @@ __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
     }
   }
   allow_next_grid();
-  constexpr bool kTwS = SGPE_COL_TW_SMEM && !TC;
-  const C* tw = a.tw;
-  if constexpr (kTwS) {
-    // (read by the second stage, after the first stage's block barrier)
-    using W = TwE<R>;
-    constexpr int kTwN = tw_offset(N, E, N);
-    W* tws = reinterpret_cast<W*>(smem_raw + col_exchange_bytes<R, N, E, COLS>());
-    for (int i = tid; i < kTwN; i += NT) tws[i] = ldg(reinterpret_cast<const W*>(a.tw) + i);
-    tw = reinterpret_cast<const C*>(tws);
-  }
-  const LineSmem<C, E, false, TC, kTwS> smv{sm + c * LS, 0, tcs};
-  if (a.fwd) fft_lines<N, E, -1, 1>(v, j, smv, tw);
+  const LineSmem<C, E, false, TC> smv{sm + c * LS, 0, tcs};
+  if (a.fwd) fft_lines<N, E, -1, 1>(v, j, smv, a.tw);
 
   R su = R(0), sw = R(0);
   if (a.nk >= 1) apply_kinetic<R, E, T>(v[0], a.k1, comp, x, j);
@@ -1093,7 +1068,7 @@ __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
     apply_kinetic<R, E, T>(v[0], a.k2, comp, x, j);
     if (a.part != nullptr) sw = thread_norm2(v[0]);
   }
-  if (a.inv) fft_lines<N, E, +1, 1>(v, j, smv, tw);
+  if (a.inv) fft_lines<N, E, +1, 1>(v, j, smv, a.tw);
   if (a.scale != R(1)) {
 #pragma unroll
     for (int m = 0; m < E; ++m) v[0][m] = cscale(v[0][m], a.scale);

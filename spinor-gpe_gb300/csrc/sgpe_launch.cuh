@@ -189,7 +189,7 @@ template <typename R, int N, int S = 0> struct ColCfg {
   static constexpr int COLS =
       cmax(cmin(S == 0 ? Tune<R>::COLS : ShapeTune<R>::cols(N, S), Tune<R>::COL_MAX_THREADS / T), 32 / T);
   static constexpr int THREADS = T * COLS;
-  static constexpr size_t SMEM = col_exchange_bytes<R, N, E, COLS>() + col_tw_bytes<R, N, E>();
+  static constexpr size_t SMEM = size_t(COLS) * (N + N / E + 2) * sizeof(Cx<R>);
   static constexpr int MINB = cmax(
       1, cmin(N % 3 == 0 ? (N >= 768 ? Tune<R>::R3_COL_MINB_LARGE : Tune<R>::R3_COL_MINB)
                          : (N >= 2048 ? Tune<R>::COL_MINB_LARGE : Tune<R>::COL_MINB),

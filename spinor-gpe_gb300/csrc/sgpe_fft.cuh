@@ -441,29 +441,6 @@ template <int P, int DIR> struct Dft3P {
 template <int DIR> struct Dft<12, DIR> : Dft3P<4, DIR> {};
 template <int DIR> struct Dft<24, DIR> : Dft3P<8, DIR> {};
 
-// Double-float radix-8 butterflies as one out-of-line function (the values
-// pass in registers): every stage of a double-float transform calls the same
-// code, so a pass kernel holds one copy instead of one per stage, which
-// keeps the large double-float kernels within the instruction caches.
-#ifndef SGPE_DF_CALL_DFT8
-#define SGPE_DF_CALL_DFT8 1
-#endif
-struct DFC8 {
-  DFC v[8];
-};
-template <int DIR> __device__ __noinline__ DFC8 dft8_df(DFC8 a) {
-  Dft<8, DIR>::run(a.v);
-  return a;
-}
-template <int DIR> __device__ __forceinline__ void dft8_call(DFC (&a)[8]) {
-  DFC8 t;
-#pragma unroll
-  for (int r = 0; r < 8; ++r) t.v[r] = a[r];
-  t = dft8_df<DIR>(t);
-#pragma unroll
-  for (int r = 0; r < 8; ++r) a[r] = t.v[r];
-}
-
 // Radix of the stage with sub-length NS of an (N, E) transform.  With P the
 // largest power of two dividing E: powers of two take stages of P (the
 // remainder last).  N = 3 * 2^k with E a multiple of 3 dividing N (E = 24 or
@@ -634,7 +611,6 @@ __device__ __forceinline__ void fft_stage(C (&v)[L][E], int j, const SM& sm, con
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
       if constexpr (SM::kTc && R == 16) tc_dft16<DIR>(a[l][q], sm.tc);
-      else if constexpr (std::is_same<C, DFC>::value && SGPE_DF_CALL_DFT8 && R == 8) dft8_call<DIR>(a[l][q]);
       else Dft<R, DIR>::run(a[l][q]);
 #pragma unroll
       for (int r = 0; r < R; ++r) renorm(a[l][q][r]);

@@ -63,12 +63,14 @@ struct SepOps {
   bool kin = false, kin_real = false;
   DevField px[2], py[2], s01x, s10x;
   bool pot = false, cpl = false;
-  // coupling, potential and coupling as one 2x2 matrix per point:
-  // C P C = pb(y) A(x), A = C diag(pa_0, kappa pa_1) C an x-table per entry,
-  // when the potential's y factors of the components differ by a constant
-  // (pb_1 = kappa pb_0); built in FP64, rounded once
-  DevField m[4], mb;
-  bool fused = false, mb_real = false;
+  // The real-space operators of the separable row kernels, one 2x2 matrix
+  // per point: coupling, potential and coupling C P C = pb(y) A(x) with
+  // A = C diag(pa_0, kappa pa_1) C (m[0..3], fused_c), or without coupling
+  // the potential alone, pb(y) diag(pa_0, kappa pa_1) (dg[0..1], fused_d);
+  // x-tables built in FP64 and rounded once, when the potential's y factors
+  // of the components differ by a constant (pb_1 = kappa pb_0)
+  DevField m[4], dg[2], mb;
+  bool fused_c = false, fused_d = false, mb_real = false;
 };
 
 // True when every value of the field has a zero imaginary part.
@@ -464,17 +466,18 @@ int build_sep_kin(sgpe_plan* p, const HostField (&a)[2], const HostField (&b)[2]
   return SGPE_OK;
 }
 
-// The fused real-space tables of SepOps (coupling, potential, coupling):
-// with c the uniform coupling diagonal, s01/s10 the off-diagonal x-tables,
-// pa_c/pb_c the potential's x and y factors and pb_1(y) = kappa pb_0(y)
-// (checked to 1e-14 over every y), C diag(pa_0 pb_0, pa_1 pb_1) C =
-// pb_0(y) A(x) with
+// The fused real-space tables of SepOps.  With c the uniform coupling
+// diagonal, s01/s10 the off-diagonal x-tables (s01 == nullptr: no coupling
+// tables), pa_c/pb_c the potential's x and y factors and pb_1(y) =
+// kappa pb_0(y) (checked to 1e-14 over every y),
+//   C diag(pa_0 pb_0, pa_1 pb_1) C = pb_0(y) A(x),
 //   A00 = c^2 d0 + s01 s10 d1,  A01 = c s01 (d0 + d1),
 //   A10 = c s10 (d0 + d1),      A11 = s10 s01 d0 + c^2 d1,
-// d0 = pa_0(x), d1 = kappa pa_1(x), all in FP64.  Leaves fused = false when
-// the y factors are not proportional.
-int build_fused(sgpe_plan* p, const HostField (&px)[2], const HostField (&py)[2], const HostField& s01,
-                const HostField& s10, double cr, double ci, SepOps* so, std::vector<void*>* allocs) {
+// and without coupling diag(pa_0 pb_0, pa_1 pb_1) = pb_0(y) diag(d0, d1),
+// d0 = pa_0(x), d1 = kappa pa_1(x), all in FP64.  Leaves both fused flags
+// false when the y factors are not proportional.
+int build_fused(sgpe_plan* p, const HostField (&px)[2], const HostField (&py)[2], const HostField* s01,
+                const HostField* s10, double cr, double ci, SepOps* so, std::vector<void*>* allocs) {
   typedef std::complex<double> cd;
   const int nx = p->nx, ny = p->ny;
   auto at = [](const HostField& f, int i) { return cd(f.v[2 * i], f.v[2 * i + 1]); };
@@ -485,32 +488,41 @@ int build_fused(sgpe_plan* p, const HostField (&px)[2], const HostField (&py)[2]
     const cd b0 = at(py[0], y), b1 = at(py[1], y);
     if (std::abs(b1 - kappa * b0) > 1e-14 * std::abs(b1) + 1e-300) return SGPE_OK;
   }
+  auto table = [&](HostField* f) {
+    f->sx = 1;
+    f->sy = 0;
+    f->v.assign(2 * (size_t)nx, 0.0);
+  };
+  auto put = [](HostField* f, int x, cd v) {
+    f->v[2 * x] = v.real();
+    f->v[2 * x + 1] = v.imag();
+  };
   const cd c(cr, ci);
-  HostField m[4], mb;
-  for (int k = 0; k < 4; ++k) {
-    m[k].sx = 1;
-    m[k].sy = 0;
-    m[k].v.assign(2 * (size_t)nx, 0.0);
-  }
+  HostField m[4], dg[2];
+  for (auto& f : m) table(&f);
+  for (auto& f : dg) table(&f);
   for (int x = 0; x < nx; ++x) {
     const cd d0 = at(px[0], x), d1 = kappa * at(px[1], x);
-    const cd a01 = at(s01, x), a10 = at(s10, x);
-    const cd v[4] = {c * c * d0 + a01 * a10 * d1, c * a01 * (d0 + d1), c * a10 * (d0 + d1),
-                     a10 * a01 * d0 + c * c * d1};
-    for (int k = 0; k < 4; ++k) {
-      m[k].v[2 * x] = v[k].real();
-      m[k].v[2 * x + 1] = v[k].imag();
+    put(&dg[0], x, d0);
+    put(&dg[1], x, d1);
+    if (s01 != nullptr) {
+      const cd a01 = at(*s01, x), a10 = at(*s10, x);
+      put(&m[0], x, c * c * d0 + a01 * a10 * d1);
+      put(&m[1], x, c * a01 * (d0 + d1));
+      put(&m[2], x, c * a10 * (d0 + d1));
+      put(&m[3], x, a10 * a01 * d0 + c * c * d1);
     }
   }
-  mb = py[0];
-  for (int k = 0; k < 4; ++k) {
-    const int rc = upload_host_field(p, m[k], &so->m[k], allocs);
-    if (rc != SGPE_OK) return rc;
-  }
-  const int rc = upload_host_field(p, mb, &so->mb, allocs);
+  int rc = upload_host_field(p, py[0], &so->mb, allocs);
+  for (int k = 0; k < 2 && rc == SGPE_OK; ++k) rc = upload_host_field(p, dg[k], &so->dg[k], allocs);
   if (rc != SGPE_OK) return rc;
-  so->mb_real = imag_zero(mb);
-  so->fused = true;
+  so->mb_real = imag_zero(py[0]);
+  so->fused_d = true;
+  if (s01 != nullptr) {
+    for (int k = 0; k < 4 && rc == SGPE_OK; ++k) rc = upload_host_field(p, m[k], &so->m[k], allocs);
+    if (rc != SGPE_OK) return rc;
+    so->fused_c = true;
+  }
   return SGPE_OK;
 }
 
@@ -595,33 +607,32 @@ template <typename R> sgpe::KinOp<R> kin_op(const SubOps& so) {
 
 template <typename R> sgpe::KinOp<R> kin_pair(const PairOps& po) { return kin_from<R>(po.a, po.b, po.sep, po.real); }
 
-// SGPE_FUSED_OPS=0 keeps coupling, potential and coupling as three
-// operators (measurements and checks); on by default.
-bool fused_ops_enabled() {
-  static const bool on = [] {
-    const char* e = std::getenv("SGPE_FUSED_OPS");
-    return !(e != nullptr && e[0] == '0');
-  }();
-  return on;
-}
+// The separable row kernels carry the fused point-wise code (SepOps::m /
+// dg); any other operator takes the generic broadcast-field kernels.
+bool fused_sep(const SubOps& so, int coupling) { return coupling ? so.sep.fused_c : so.sep.fused_d; }
 
 template <typename R> sgpe::RealOp<R> real_op(const SubOps& so, int coupling) {
   sgpe::RealOp<R> o;
-  const bool sep = so.sep.pot && (!coupling || so.sep.cpl);
+  const bool sep = fused_sep(so, coupling);
   for (int c = 0; c < 2; ++c) {
-    o.pa[c] = typed<R>(sep ? so.sep.px[c] : so.pot_a[c]);
-    o.pb[c] = typed<R>(sep ? so.sep.py[c] : so.pot_b[c]);
+    o.pa[c] = typed<R>(so.pot_a[c]);
+    o.pb[c] = typed<R>(so.pot_b[c]);
   }
   o.cc = typed<R>(so.cc);
   o.cs = typed<R>(so.cs);
   o.ce = typed<R>(so.ce);
   o.has_s01 = so.has_s01 ? 1 : 0;
-  o.s01 = typed<R>(sep && coupling ? so.sep.s01x : so.has_s01 ? so.s01 : so.cs);
-  o.s10 = typed<R>(sep && coupling ? so.sep.s10x : so.has_s01 ? so.s10 : so.cs);
+  o.s01 = typed<R>(so.has_s01 ? so.s01 : so.cs);
+  o.s10 = typed<R>(so.has_s01 ? so.s10 : so.cs);
   o.sep = sep ? 1 : 0;
-  o.fused = (sep && coupling && so.sep.fused && fused_ops_enabled()) ? 1 : 0;
-  if (o.fused) {
-    for (int k = 0; k < 4; ++k) o.m[k] = typed<R>(so.sep.m[k]);
+  o.diag = coupling ? 0 : 1;
+  if (sep) {
+    if (coupling) {
+      for (int k = 0; k < 4; ++k) o.m[k] = typed<R>(so.sep.m[k]);
+    } else {
+      o.m[0] = o.m[1] = o.m[2] = typed<R>(so.sep.dg[0]);  // m[1], m[2] unread
+      o.m[3] = typed<R>(so.sep.dg[1]);
+    }
     o.mb = typed<R>(so.sep.mb);
     o.real_mb = so.sep.mb_real ? 1 : 0;
   }
@@ -1426,9 +1437,10 @@ int sgpe_set_substep(sgpe_plan* p, int sub, const sgpe_substep_ops* ops) {
       if (rc == SGPE_OK) rc = upload_host_field(p, s10x, &so.sep.s10x, &so.allocs);
       so.sep.cpl = (rc == SGPE_OK);
     }
-    if (rc == SGPE_OK && so.sep.pot && so.sep.cpl) {
+    if (rc == SGPE_OK && so.sep.pot) {
       const HostField hc = host_field(ops->cpl_c);
-      rc = build_fused(p, px, py, s01x, s10x, hc.v[0], hc.v[1], &so.sep, &so.allocs);
+      rc = build_fused(p, px, py, so.sep.cpl ? &s01x : nullptr, so.sep.cpl ? &s10x : nullptr, hc.v[0],
+                       hc.v[1], &so.sep, &so.allocs);
     }
     if (rc != SGPE_OK) {
       free_sub(so);
@@ -1943,7 +1955,7 @@ void build_groups(sgpe_batch* b) {
       if (q->tc) return false;  // the grouped kernels carry the FP32 DFTs
       if (q->bits == SGPE_DTYPE_DF) return false;  // no grouped double-float kernels
       for (int sub = 0; sub < 2; ++sub)
-        if (!(q->sub[sub].sep.pot && (!q->coupling || q->sub[sub].sep.cpl))) return false;
+        if (!fused_sep(q->sub[sub], q->coupling)) return false;
       return true;
     };
     if (!b->grouping || !sep(p)) continue;

@@ -154,10 +154,12 @@ template <typename R> struct RealOp {
   // zero imaginary parts (imaginary time): real multiplies give the same bits
   int real_pot, real_cc;
   R zr, zi;
-  // fused (with sep and coupling): coupling, potential and coupling as
-  // pb(y) A(x), m[0..3] = A00, A01, A10, A11 x-tables of Nx values, mb the
-  // y-table of Ny values (real_mb: zero imaginary parts)
-  int fused, real_mb;
+  // sep: the separable row kernels apply coupling, potential and coupling
+  // as one matrix per point, pb(y) A(x) with m[0..3] = A00, A01, A10, A11
+  // x-tables of Nx values and mb the y-table of Ny values; diag: no
+  // coupling, A = diag(m[0], m[3]) (m[1], m[2] unread); real_mb: mb has zero
+  // imaginary parts
+  int diag, real_mb;
   Field<R> m[4], mb;
 };
 
@@ -647,8 +649,9 @@ __device__ __forceinline__ void apply_real_ops(Cx<R>& p0, Cx<R>& p1, const Point
 }
 
 // The same with coupling, potential and coupling applied as one 2x2 matrix
-// per point, pb(y) A(x) (RealOp::fused): interaction, A, then pb times the
-// interaction again (pb is a scalar for both components, so it commutes).
+// per point, pb(y) A(x) (the separable kernels, RealOp::sep): interaction,
+// A, then pb times the interaction again (pb is a scalar for both
+// components, so it commutes).
 template <typename R>
 __device__ __forceinline__ void apply_fused_ops(Cx<R>& p0, Cx<R>& p1, const Cx<R> (&m)[4], Cx<R> pb,
                                                 const RowArgs<R>& a) {
@@ -667,8 +670,14 @@ __device__ __forceinline__ void apply_fused_ops(Cx<R>& p0, Cx<R>& p1, const Cx<R
     p0 = cmul(p0, i0);
     p1 = cmul(p1, i1);
   }
-  const C q0 = cadd(cmul(m[0], p0), cmul(m[1], p1));
-  const C q1 = cadd(cmul(m[2], p0), cmul(m[3], p1));
+  C q0, q1;
+  if (op.diag) {
+    q0 = cmul(m[0], p0);
+    q1 = cmul(m[3], p1);
+  } else {
+    q0 = cadd(cmul(m[0], p0), cmul(m[1], p1));
+    q1 = cadd(cmul(m[2], p0), cmul(m[3], p1));
+  }
   if (ireal && op.real_mb) {
     p0 = cscale(q0, i0.x * pb.x);
     p1 = cscale(q1, i1.x * pb.x);
@@ -876,49 +885,29 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
       auto at0 = [&](int m, int x) -> C& { return kOpsFold ? q0[m * kStep] : r0.line(0)[LS0::pad(unsigned(x))]; };
       auto at1 = [&](int m, int x) -> C& { return kOpsFold ? q1[m * kStep] : r1.line(0)[LS0::pad(unsigned(x))]; };
       if constexpr (SEP) {
-       if (a.coupling && a.op.fused) {
-        // coupling, potential, coupling as pb(y) A(x): four x-tables read at
-        // jj + m*2T, the row's pb hoisted
+        // separable operators as pb(y) A(x): the x-tables read at jj + m*2T
+        // (compile-time offsets from one base), the row's pb hoisted
         const C pb = ldg(a.op.mb.p + y);
         const C* m0 = a.op.m[0].p + jj;
         const C* m1 = a.op.m[1].p + jj;
         const C* m2 = a.op.m[2].p + jj;
         const C* m3 = a.op.m[3].p + jj;
+        const bool diag = a.op.diag != 0;
 #pragma unroll ops_unroll<R>()
         for (int m = 0; m < E / 2; ++m) {
           const int x = jj + m * 2 * T;
           C p0 = cscale(at0(m, x), lam), p1 = cscale(at1(m, x), lam);
-          const C mm[4] = {ldg(m0 + m * 2 * T), ldg(m1 + m * 2 * T), ldg(m2 + m * 2 * T), ldg(m3 + m * 2 * T)};
+          C mm[4];
+          mm[0] = ldg(m0 + m * 2 * T);
+          mm[3] = ldg(m3 + m * 2 * T);
+          if (!diag) {
+            mm[1] = ldg(m1 + m * 2 * T);
+            mm[2] = ldg(m2 + m * 2 * T);
+          }
           apply_fused_ops<R>(p0, p1, mm, pb, a);
           at0(m, x) = p0;
           at1(m, x) = p1;
         }
-       } else {
-        // separable operators: x-tables read at jj + m*2T (compile-time
-        // offsets from one base), row values and the uniform c hoisted
-        PointOps<R> v;
-        v.pb0 = ldg(a.op.pb[0].p + y);
-        v.pb1 = ldg(a.op.pb[1].p + y);
-        v.cc = a.coupling ? ldg(a.op.cc.p) : C{};
-        const C* pa0 = a.op.pa[0].p + jj;
-        const C* pa1 = a.op.pa[1].p + jj;
-        const C* s01 = a.op.s01.p + jj;
-        const C* s10 = a.op.s10.p + jj;
-#pragma unroll ops_unroll<R>()
-        for (int m = 0; m < E / 2; ++m) {
-          const int x = jj + m * 2 * T;
-          C p0 = cscale(at0(m, x), lam), p1 = cscale(at1(m, x), lam);
-          v.pa0 = ldg(pa0 + m * 2 * T);
-          v.pa1 = ldg(pa1 + m * 2 * T);
-          if (a.coupling) {
-            v.s01 = ldg(s01 + m * 2 * T);
-            v.s10 = ldg(s10 + m * 2 * T);
-          }
-          apply_real_ops<R>(p0, p1, v, a);
-          at0(m, x) = p0;
-          at1(m, x) = p1;
-        }
-       }
       } else {
         RowFields<R> rf;
         rf.init(a.op, y);

@@ -706,7 +706,8 @@ def run_served(args, world, rank, local):
                    'requests_per_s': st['served'] / wall,
                    'peak_active': st['peak_active'],
                    'peak_admitted_bytes': st['peak_admitted_bytes'],
-                   'by_kind': kinds},
+                   'by_kind': kinds,
+                   'host_loop': st['host']},
         'sequential_plain': {'value': world * seq_gps / t_seq,
                              'unit': 'grid-point-steps/s',
                              'device_s': t_seq, 'requests': len(seq),

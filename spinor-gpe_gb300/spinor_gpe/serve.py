@@ -189,7 +189,12 @@ class SolveServer:
     def run(self, requests, realtime=True):
         """Serve ``requests`` (any order; each becomes visible at its
         ``arrival`` time when ``realtime``, else all at once) and return the
-        results in request order.  Fills ``self.stats``."""
+        results in request order.  Fills ``self.stats``; its ``host`` entry
+        gives the loop's own cost: chunks submitted, seconds spent queueing
+        them (``enqueue_s``) and reading their results (``process_s``),
+        seconds asleep waiting for the GPU (``asleep_s``) and the longest
+        loop iteration spent working, during which no finished solve is
+        resubmitted."""
         for r in requests:
             if r.footprint > self.hbm_cap:
                 raise ValueError(f'request {r.rid} needs {r.footprint} bytes, '
@@ -214,9 +219,16 @@ class SolveServer:
         releases = 0
         pool = concurrent.futures.ThreadPoolExecutor(
             max_workers=self.build_workers)
+        # host-side cost of the loop: time in chunk submission and result
+        # reads, time asleep waiting for the GPU, longest busy iteration
+        t_enqueue = t_process = t_sleep = 0.0
+        chunks = iterations = 0
+        busy_max = 0.0
         t0 = self.clock()
         while arrivals or pending or building or active:
-            now = self.clock() - t0
+            iterations += 1
+            t_iter = self.clock()
+            now = t_iter - t0
             while arrivals and (not realtime or arrivals[0].arrival <= now):
                 pending.append(arrivals.popleft())
             if self.max_queue_s is not None:
@@ -243,7 +255,10 @@ class SolveServer:
                 req, stream, t_adm = building.pop(fut)
                 solve = _Solve(req, fut.result(), stream, self.device)
                 solve.admitted = t_adm
+                t_a = self.clock()
                 solve.enqueue()
+                t_enqueue += self.clock() - t_a
+                chunks += 1
                 active.append(solve)
                 progressed = True
             peak_active = max(peak_active, len(active))
@@ -253,7 +268,10 @@ class SolveServer:
                     still.append(s)
                     continue
                 progressed = True
-                if s.process():
+                t_a = self.clock()
+                finished = s.process()
+                t_process += self.clock() - t_a
+                if finished:
                     t_fin = self.clock() - t0
                     psik = None
                     if self.keep_psik:
@@ -269,14 +287,20 @@ class SolveServer:
                     parked_bytes += s.req.footprint
                     free_streams.append(s.stream)
                 else:
+                    t_a = self.clock()
                     s.enqueue()
+                    t_enqueue += self.clock() - t_a
+                    chunks += 1
                     still.append(s)
             active = still
+            t_a = self.clock()
+            busy_max = max(busy_max, t_a - t_iter)
             if not progressed:
                 if not active and not building and arrivals and realtime:
                     time.sleep(max(0.0, min(arrivals[0].arrival - now, 0.01)))
                 else:
                     time.sleep(20e-6)
+                t_sleep += self.clock() - t_a
         torch.cuda.synchronize(self.device)
         wall = self.clock() - t0
         pool.shutdown(wait=True)
@@ -293,7 +317,12 @@ class SolveServer:
                       'p99_ms': float(np.percentile(lat, 99) * 1e3),
                       'peak_active': peak_active,
                       'peak_admitted_bytes': peak_used,
-                      'parked_releases': releases}
+                      'parked_releases': releases,
+                      'host': {'chunks': chunks, 'iterations': iterations,
+                               'enqueue_s': t_enqueue, 'process_s': t_process,
+                               'asleep_s': t_sleep,
+                               'busy_s': wall - t_sleep,
+                               'longest_busy_iteration_ms': 1e3 * busy_max}}
         return res
 
 

@@ -69,6 +69,12 @@ def test_results_same_alone_and_in_the_mix(tmp_path):
     mix = serve.SolveServer(max_active=3, keep_psik=True)
     together = mix.run(reqs, realtime=True)
     assert mix.stats['peak_active'] <= 3
+    # the loop's own accounting: one submission per chunk of every solve
+    host = mix.stats['host']
+    assert host['chunks'] == sum(-(-got.steps // req.chunk) for req, got in zip(reqs, together))
+    assert 0.0 <= host['enqueue_s'] <= host['busy_s']
+    assert 0.0 <= host['process_s'] <= host['busy_s']
+    assert host['busy_s'] + host['asleep_s'] == pytest.approx(mix.stats['wall_s'])
     for req, got in zip(reqs, together):
         alone = serve.SolveServer(max_active=1, keep_psik=True).run([req])[0]
         assert (alone.steps, alone.converged) == (got.steps, got.converged)

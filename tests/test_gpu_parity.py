@@ -532,3 +532,24 @@ def test_device_analysis_matches_numpy(tp, tmp_path, dtype):
     assert abs(d['separation'] - ref.calc_separation()) <= 1e-6
     res = prop.prop_loop(5)
     assert abs(res.calc_separation() - prop.analysis()['separation']) <= 1e-12
+
+
+def test_stream_handle_follows_the_current_stream(tp):
+    """The stream handle given to every C call is the caller's current
+    stream (default, or one selected with ``torch.cuda.stream``), for a
+    device given as torch.device, string or index."""
+    import ctypes
+    from spinor_gpe.pspinor import _native
+
+    def handle(d):
+        h = _native._stream(torch, d)
+        return h.value if isinstance(h, ctypes.c_void_p) else h
+
+    dev = torch.device('cuda', torch.cuda.current_device())
+    torch.empty(1, device=dev)
+    assert handle(dev) == torch.cuda.current_stream(dev).cuda_stream
+    side = torch.cuda.Stream(dev)
+    with torch.cuda.stream(side):
+        for d in (dev, 'cuda', f'cuda:{dev.index}', dev.index):
+            assert handle(d) == side.cuda_stream
+    assert handle(dev) == torch.cuda.current_stream(dev).cuda_stream

@@ -553,3 +553,49 @@ def test_stream_handle_follows_the_current_stream(tp):
         for d in (dev, 'cuda', f'cuda:{dev.index}', dev.index):
             assert handle(d) == side.cuda_stream
     assert handle(dev) == torch.cuda.current_stream(dev).cuda_stream
+
+
+@pytest.mark.parametrize('shape', [(4096, 4096), (2048, 4096)])
+@pytest.mark.parametrize('dtype', [64, 128, 'double-float'])
+def test_largest_grids_match_oracle(tp, tmp_path, shape, dtype):
+    """Real-time Raman-dressed steps at the largest supported grids against
+    the complex128 oracle (run on the same GPU): 1e-5 for complex64, 1e-10
+    for complex128 and double-float."""
+    from spinor_gpe import workloads
+    from spinor_gpe.pspinor import pspinor as spin
+    from spinor_gpe.pspinor import tensor_tools as ttools
+    ny, nx = shape
+    ps = workloads.build(spin.PSpinor, ttools.fft_2d, str(tmp_path / 'x') + '/',
+                         nx=nx, ny=ny, half_x=nx * 0.0625 / 2,
+                         half_y=ny * 0.0625 / 2, g=(1000.0, 995.0, 990.0),
+                         omega=1.0, k_l=3.0, delta=0.3, seed=6)
+    n = 3
+    orc = OraclePropagator(_inputs_from_spin(ps), 1e-3, 'real', 128, device='cuda')
+    for _ in range(n):
+        orc.full_step()
+    ref = orc.psik_numpy()
+    del orc
+    prop = tp.TensorPropagator(ps, 1e-3, n, 'cuda', time='real', dtype=dtype)
+    prop.full_steps(n)
+    got = np.array([t.cpu().numpy() for t in prop.psik]).astype(np.complex128)
+    assert rel_l2(got, ref) <= (1e-5 if dtype == 64 else 1e-10)
+
+
+@pytest.mark.parametrize('dtype', [64, 128, 'double-float'])
+def test_zero_and_negative_step_counts(tp, tmp_path, dtype):
+    """Zero steps (with or without an empty populations buffer) leave the
+    state bit-for-bit as it was; a negative count is an argument error."""
+    case = CASES['imag_raman_64']
+    p = case_params(case)
+    prop = tp.TensorPropagator(spin_from_case(case, tmp_path), p['dt'], 1, 'cuda',
+                               time=p['time'], dtype=dtype)
+    prop.full_steps(2)
+    before = np.array([t.cpu().numpy() for t in prop.psik])
+    prop.full_steps(0)
+    prop.full_steps(0, torch.empty((0, 2), dtype=torch.float64, device='cuda'))
+    after = np.array([t.cpu().numpy() for t in prop.psik])
+    np.testing.assert_array_equal(before, after)
+    with pytest.raises(_native_error()):
+        prop.full_steps(-1)
+    prop.full_steps(1)
+    assert rel_l2(np.array([t.cpu().numpy() for t in prop.psik]), before) > 0

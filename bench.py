@@ -90,6 +90,12 @@ def parse():
     ap.add_argument('--kernel-shapes', type=int, nargs=2, default=None, metavar=('ROW', 'COL'),
                     help='raman_quench: run the solves in these kernel shapes instead of the '
                          'defaults (sgpe_shape_count lists them)')
+    ap.add_argument('--batch-sizes', type=int, nargs='+', default=None,
+                    help='batched_uneven: draw the grid sides from these (default '
+                         '128 192 256 384 512 768 1024)')
+    ap.add_argument('--batch-queue', action='store_true',
+                    help='batched_uneven: step the batch with the work-queue kernel (one '
+                         'persistent launch per graph) instead of grouped launches')
     ap.add_argument('--no-batch-autotune', action='store_true',
                     help='batched_uneven: keep every solve in its default kernel shapes '
                          '(no PropagatorBatch.autotune)')
@@ -474,6 +480,9 @@ def run_native(args, world, rank, local):
                            'PropagatorBatch (autotuned kernel shapes) against the '
                            'same solves one after another (bench.py --workload '
                            'batched_uneven runs it alone)'}
+        if b.get('work_queue'):
+            batched['work_queue'] = {k: b['work_queue'][k] for k in
+                                     ('value', 'speedup_vs_sequential', 'what')}
 
     line = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world,
@@ -542,13 +551,14 @@ def run_batched(args, world, rank, local):
     a branch per solve), against the plain single-solve drop-in stepping the
     same solves one after another.  Metric: aggregate grid-point-steps/s."""
     line = measure_batched(world, rank, local, args.solves, args.batch_steps,
-                           args.warmup, not args.no_batch_autotune, args.breakdown)
+                           args.warmup, not args.no_batch_autotune and not args.batch_queue,
+                           args.breakdown, queue=args.batch_queue, sizes=args.batch_sizes)
     if rank == 0:
         print(json.dumps(line))
 
 
 def measure_batched(world, rank, local, n_solves, k, warmup, autotune=True,
-                    with_breakdown=False):
+                    with_breakdown=False, queue=False, sizes=None):
     """The batched-uneven measurement (see ``run_batched``); returns its JSON
     line as a dict."""
     import torch
@@ -560,8 +570,9 @@ def measure_batched(world, rank, local, n_solves, k, warmup, autotune=True,
     torch.cuda.set_device(local)
     device = f'cuda:{local}'
     tmp = tempfile.mkdtemp(prefix='sgpe_batch_')
+    extra = {} if sizes is None else {'sizes': tuple(sizes)}
     spins = workloads.batched_uneven(spin.PSpinor, ttools.fft_2d, tmp + '/',
-                                     n_solves=n_solves, seed=4 + rank)
+                                     n_solves=n_solves, seed=4 + rank, **extra)
     props = [tprop.TensorPropagator(s, 0.02, k, device, time='imag', dtype=64)
              for s in spins]
     points = sum(s.psik[0].size for s in spins)
@@ -599,7 +610,7 @@ def measure_batched(world, rank, local, n_solves, k, warmup, autotune=True,
                                  'sequential_us': 1e6 * t_one * len(cls),
                                  'batched_us': 1e6 * t_grp}
 
-    batch = PropagatorBatch(props)
+    batch = PropagatorBatch(props, queue=queue)
     tuned = None
     if autotune:
         # kernel shapes per size class for grouped stepping (set-up, untimed)
@@ -614,8 +625,26 @@ def measure_batched(world, rank, local, n_solves, k, warmup, autotune=True,
     batch.full_steps(max(warmup, 9))
     with ClockSampler(local) as clk:
         t_bat = timed(lambda: batch.full_steps(k))
+    if queue:
+        batch.check_device()
     for p in props[:4]:
         assert all(torch.isfinite(c).all().item() for c in p.psik)
+    work_queue = None
+    if not queue:
+        # the same solves through the work-queue kernel (one persistent
+        # launch per 8 steps), beside the grouped launches
+        batch.close()
+        qb = PropagatorBatch(props, queue=True)
+        qb.full_steps(max(warmup, 9))
+        t_q = timed(lambda: qb.full_steps(k))
+        qb.check_device()
+        qb.close()
+        work_queue = {'value': world * points * k / t_q, 'unit': 'grid-point-steps/s',
+                      'ms_per_step': 1e3 * t_q / k,
+                      'speedup_vs_sequential': t_seq / t_q,
+                      'what': 'PropagatorBatch(queue=True): one persistent cooperative '
+                              'launch per 8 steps whose blocks claim pass items from a '
+                              'device work queue'}
     sizes = {}
     for s in spins:
         sizes[s.psik[0].shape[0]] = sizes.get(s.psik[0].shape[0], 0) + 1
@@ -645,8 +674,11 @@ def measure_batched(world, rank, local, n_solves, k, warmup, autotune=True,
             f'{ny}x{nx}': list(props[[p._shape for p in props].index((ny, nx))].kernel_shapes)
             for (_, ny, nx) in tuned}),
         'batch_autotune_s': None if tuned is None else tune_s,
-        'gpu_launches': 6 * k * n_solves,
+        'batch_mode': ('work queue: one persistent launch per graph (8 steps)' if queue
+                       else 'grouped launches per size class, parallel graph branches'),
+        'gpu_launches': (-(-k // 8) if queue else 6 * k * n_solves),
         'per_class_step_us': breakdown,
+        'work_queue': work_queue,
         'clocks': clk.summary(),
     }
     batch.close()

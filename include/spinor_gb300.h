@@ -240,6 +240,30 @@ int sgpe_batch_destroy(sgpe_batch* batch);
  * stepping each plan alone with sgpe_full_steps. */
 int sgpe_batch_steps(sgpe_batch* batch, int n_steps, void* stream);
 
+/* Work-queue mode of a batch (on = 1): its steps run as one persistent
+ * (cooperative) launch per graph, fed from a device work queue: every pass
+ * of every sub-step of every solve is split into items (column tiles, row
+ * groups), blocks claim the items in one global order, and an item waits
+ * (bounded, 1 s) until the previous pass of its solve has finished.  The
+ * launch is captured in the batch's CUDA graphs (launched directly when
+ * the driver refuses the capture).  Complex64 plans with separable
+ * operators and sides 128, 192, 256, 384, 512, 768 or 1024 only
+ * (SGPE_ERR_ARG otherwise).  The items use their own tile shapes, so
+ * results agree with sgpe_full_steps per plan to complex64 rounding (not
+ * bit for bit).  on = 0 returns to grouped launches.  No counterpart in
+ * the original (one solve per process). */
+int sgpe_batch_set_queue(sgpe_batch* batch, int on);
+
+/* Error word of the batch's work queue: 0, or the code of a wait that gave
+ * up (the batch's states are then not reliable; SGPE_ERR_CUDA).
+ * Synchronous (a 4-byte device read). */
+int sgpe_batch_device_status(sgpe_batch* batch, int* status);
+
+/* Check of the work queue's bounded wait on the current device: one block
+ * waits for a counter that nothing increments; gave_up = 1 when the wait
+ * ended by its limit (about 1 s, returned in waited_ms). */
+int sgpe_check_queue_wait(int* gave_up, double* waited_ms);
+
 /* Arithmetic of the radix-16 DFT stages of the plan's transforms:
  * mode 0 (default) FP32 butterflies on the CUDA cores; mode 1 split-BF16
  * products on the tensor cores (each FP32 operand split into BF16 head and

@@ -24,6 +24,7 @@
 #include "sgpe_analysis.cuh"
 #include "sgpe_energy.cuh"
 #include "sgpe_launch.cuh"
+#include "sgpe_queue.cuh"
 #include "spinor_gb300.h"
 
 namespace {
@@ -225,6 +226,20 @@ struct sgpe_batch {
   std::vector<unsigned long long> groups_epoch;    // plans' epochs when built
   bool groups_built = false;
   bool grouping = true;                            // SGPE_BATCH_GROUPING=0 disables
+  // Work-queue mode (sgpe_batch_set_queue): the steps run as one persistent
+  // launch of the queue kernel per graph (sgpe_queue.cuh) instead of
+  // grouped launches in parallel branches.
+  bool queue = false;
+  bool q_built = false;
+  bool q_direct = false;             // the launch could not be captured: launched directly
+  int q_grid = 0;                    // resident blocks of the queue kernel
+  void* q_solves = nullptr;          // device QueueSolve[n]
+  void* q_col = nullptr;             // device ColArgs<float>[n][3]
+  void* q_row = nullptr;             // device RowArgs<float>[n][2]
+  int* q_first = nullptr;            // device [2][n + 1]: first column / row item of each solve
+  unsigned* q_words = nullptr;       // device: error word, claim, abort, done[n][6 * kGraphSteps]
+  void* q_tw[sgpe::kQueueClasses] = {};  // twiddle tables of the queue shapes per line length
+  std::vector<unsigned long long> q_epoch;  // plans' epochs when the arguments were built
 };
 
 namespace {
@@ -1879,12 +1894,26 @@ void free_groups(sgpe_batch* b) {
 }
 }  // namespace
 
+namespace {
+void free_queue_args(sgpe_batch* b) {
+  for (void* x : {b->q_solves, b->q_col, b->q_row, static_cast<void*>(b->q_first)})
+    if (x) cudaFree(x);
+  b->q_solves = b->q_col = b->q_row = nullptr;
+  b->q_first = nullptr;
+  b->q_built = false;
+}
+}  // namespace
+
 int sgpe_batch_destroy(sgpe_batch* b) {
   if (b == nullptr) return SGPE_OK;
   DeviceGuard g(b->device);
   for (auto& x : b->graph)
     if (x) cudaGraphExecDestroy(x);
   free_groups(b);
+  free_queue_args(b);
+  if (b->q_words) cudaFree(b->q_words);
+  for (void* t : b->q_tw)
+    if (t) cudaFree(t);
   for (auto& ev : b->joins)
     if (ev) cudaEventDestroy(ev);
   if (b->fork) cudaEventDestroy(b->fork);
@@ -2046,6 +2075,141 @@ int capture_batch(sgpe_batch* b, int steps, cudaGraphExec_t* out) {
   return SGPE_OK;
 }
 
+// Why plan p cannot run in the queue kernel (nullptr: it can): complex64
+// FP32 transforms with the fused separable operators, sides among the
+// queue's line lengths, and tiles that divide the grid.
+const char* queue_unsupported(const sgpe_plan* p) {
+  if (p->bits != 64) return "the work queue runs complex64 plans only";
+  if (p->tc) return "the work queue runs the FP32 transforms only";
+  for (int sub = 0; sub < 2; ++sub)
+    if (!fused_sep(p->sub[sub], p->coupling)) return "the work queue needs separable operators";
+  if (sgpe::queue_class(p->nx) < 0 || sgpe::queue_class(p->ny) < 0)
+    return "the work queue takes sides 128, 192, 256, 384, 512, 768 and 1024";
+  if (p->nx % sgpe::queue_cols(p->ny) != 0 || p->ny % sgpe::queue_rows(p->nx) != 0)
+    return "the work queue's tiles do not divide this grid";
+  return nullptr;
+}
+
+// Device arguments of the queue kernel: per solve the column-pass arguments
+// of the three sub-steps and the row-pass arguments of the two sub-step
+// kinds (the plans' own, with the queue shapes' twiddle tables and tile
+// counts), and the first item of each solve in a column and a row phase.
+int queue_build(sgpe_batch* b) {
+  free_queue_args(b);
+  const int n = int(b->plans.size());
+  std::vector<sgpe::ColArgs<float>> col(3 * n);
+  std::vector<sgpe::RowArgs<float>> row(2 * n);
+  std::vector<sgpe::QueueSolve> sv(n);
+  std::vector<int> first(2 * (n + 1), 0);
+  const int prevs[3] = {0, 0, 1}, subs[3] = {0, 1, 0};
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < n && e == cudaSuccess; ++i) {
+    sgpe_plan* p = b->plans[i];
+    const int cx = sgpe::queue_class(p->nx), cy = sgpe::queue_class(p->ny);
+    for (int c : {cx, cy})
+      if (b->q_tw[c] == nullptr && e == cudaSuccess) {
+        const int len = sgpe::queue_size(c);
+        b->q_tw[c] = upload_twiddles<float>(len, sgpe::queue_e(len), &e);
+      }
+    if (e != cudaSuccess) break;
+    const int tiles = p->nx / sgpe::queue_cols(p->ny);
+    const int rows = p->ny / sgpe::queue_rows(p->nx);
+    const int saved = p->prev_sub;
+    bool ok = true;
+    for (int v = 0; v < 3 && ok; ++v) {
+      p->prev_sub = prevs[v];
+      ok = col_step_args<float>(p, subs[v], false, &col[3 * i + v]);
+      col[3 * i + v].tw = static_cast<const float2*>(b->q_tw[cy]);
+      col[3 * i + v].tmap = nullptr;
+    }
+    p->prev_sub = saved;
+    if (!ok) return fail(SGPE_ERR_OOM, "work queue: merged kinetic tables");
+    for (int sub = 0; sub < 2; ++sub) {
+      row[2 * i + sub] = row_step_args<float>(p, sub, nullptr);
+      row[2 * i + sub].tw = static_cast<const float2*>(b->q_tw[cx]);
+      row[2 * i + sub].ntile = tiles;
+    }
+    sv[i].cls_x = cx;
+    sv[i].cls_y = cy;
+    sv[i].col_tiles = tiles;
+    sv[i].row_items = rows;
+    first[i + 1] = first[i] + 2 * tiles;
+    first[(n + 1) + i + 1] = first[(n + 1) + i] + rows;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "work queue twiddles");
+  e = cudaMalloc(&b->q_col, sizeof(sgpe::ColArgs<float>) * col.size());
+  if (e == cudaSuccess) e = cudaMalloc(&b->q_row, sizeof(sgpe::RowArgs<float>) * row.size());
+  if (e == cudaSuccess) e = cudaMalloc(&b->q_solves, sizeof(sgpe::QueueSolve) * sv.size());
+  if (e == cudaSuccess) e = cudaMalloc(&b->q_first, sizeof(int) * first.size());
+  if (e == cudaSuccess) {
+    for (int i = 0; i < n; ++i) {
+      sv[i].col = static_cast<const sgpe::ColArgs<float>*>(b->q_col) + 3 * i;
+      sv[i].row = static_cast<const sgpe::RowArgs<float>*>(b->q_row) + 2 * i;
+    }
+    e = cudaMemcpy(b->q_col, col.data(), sizeof(sgpe::ColArgs<float>) * col.size(), cudaMemcpyHostToDevice);
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->q_row, row.data(), sizeof(sgpe::RowArgs<float>) * row.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->q_solves, sv.data(), sizeof(sgpe::QueueSolve) * sv.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b->q_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    free_queue_args(b);
+    return cuda_fail(e, "work queue arguments");
+  }
+  b->q_built = true;
+  b->q_epoch.clear();
+  for (const sgpe_plan* p : b->plans) b->q_epoch.push_back(p->epoch);
+  return SGPE_OK;
+}
+
+// Enqueue `steps` steps as one launch of the queue kernel on s: reset the
+// claim counter, the abort flag and the finished-item counters, then launch.
+cudaError_t queue_enqueue(sgpe_batch* b, int steps, cudaStream_t s) {
+  const int n = int(b->plans.size());
+  sgpe::QueueArgs q{};
+  q.solves = static_cast<const sgpe::QueueSolve*>(b->q_solves);
+  q.col_first = b->q_first;
+  q.row_first = b->q_first + (n + 1);
+  q.n = n;
+  q.phases = 6 * steps;
+  q.err = reinterpret_cast<int*>(b->q_words);
+  q.claim = b->q_words + 1;
+  q.abort = reinterpret_cast<int*>(b->q_words + 2);
+  q.done = b->q_words + 3;
+  cudaError_t e =
+      cudaMemsetAsync(b->q_words + 1, 0, sizeof(unsigned) * (2 + size_t(n) * 6 * kGraphSteps), s);
+  if (e == cudaSuccess) e = sgpe::launch_batch_queue(q, b->q_grid, s);
+  return e;
+}
+
+// Capture `steps` queue steps as a graph (the cooperative launch as a
+// kernel node); when the capture is refused the steps are launched directly.
+int capture_queue(sgpe_batch* b, int steps, cudaGraphExec_t* out) {
+  cudaError_t e = cudaStreamBeginCapture(b->root, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return cuda_fail(e, "queue begin capture");
+  const cudaError_t el = queue_enqueue(b, steps, b->root);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(b->root, &graph);
+  if (el != cudaSuccess || e2 != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    b->q_direct = true;
+    return SGPE_OK;
+  }
+  e = cudaGraphInstantiate(out, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    b->q_direct = true;
+    return SGPE_OK;
+  }
+  std::vector<unsigned long long>& ep = b->epoch[steps == 1 ? 0 : 1];
+  ep.clear();
+  for (sgpe_plan* p : b->plans) ep.push_back(p->epoch);
+  return SGPE_OK;
+}
+
 // True when some plan's physics or operators changed since graph k was
 // captured.
 bool batch_stale(const sgpe_batch* b, int k) {
@@ -2078,21 +2242,94 @@ int sgpe_batch_steps(sgpe_batch* b, int n_steps, void* stream) {
     }
     done = 1;
   }
+  if (b->queue && done < n_steps) {
+    std::vector<unsigned long long> now;
+    for (const sgpe_plan* p : b->plans) now.push_back(p->epoch);
+    if (!b->q_built || b->q_epoch != now) {
+      for (auto& x : b->graph)
+        if (x != nullptr) {
+          cudaGraphExecDestroy(x);
+          x = nullptr;
+        }
+      for (sgpe_plan* p : b->plans)
+        for (int x = 0; x < 2; ++x)
+          for (int y = 0; y < 2; ++y)
+            if (ensure_pair(p, x, y) != SGPE_OK) return fail(SGPE_ERR_OOM, "work queue: merged kinetic tables");
+      cudaError_t e = cudaStreamSynchronize(s);  // launches still reading the old arguments
+      if (e != cudaSuccess) return cuda_fail(e, "work queue rebuild");
+      const int rc = queue_build(b);
+      if (rc != SGPE_OK) return rc;
+    }
+  }
   while (done < n_steps) {
     const int k = (n_steps - done >= kGraphSteps) ? 1 : 0;
     if (b->graph[k] != nullptr && batch_stale(b, k)) {
       cudaGraphExecDestroy(b->graph[k]);
       b->graph[k] = nullptr;
     }
+    if (b->queue && b->q_direct) {
+      const cudaError_t e = queue_enqueue(b, k ? kGraphSteps : 1, s);
+      if (e != cudaSuccess) return cuda_fail(e, "work queue launch");
+      done += k ? kGraphSteps : 1;
+      continue;
+    }
     if (b->graph[k] == nullptr) {
-      const int rc = capture_batch(b, k ? kGraphSteps : 1, &b->graph[k]);
+      const int rc = b->queue ? capture_queue(b, k ? kGraphSteps : 1, &b->graph[k])
+                              : capture_batch(b, k ? kGraphSteps : 1, &b->graph[k]);
       if (rc != SGPE_OK) return rc;
+      if (b->queue && b->q_direct) continue;
     }
     const cudaError_t e = cudaGraphLaunch(b->graph[k], s);
     if (e != cudaSuccess) return cuda_fail(e, "batch graph launch");
     done += k ? kGraphSteps : 1;
   }
   return SGPE_OK;
+}
+
+int sgpe_batch_set_queue(sgpe_batch* b, int on) {
+  if (b == nullptr) return fail(SGPE_ERR_ARG, "null batch");
+  DeviceGuard g(b->device);
+  if (on) {
+    for (const sgpe_plan* p : b->plans)
+      if (const char* why = queue_unsupported(p)) return fail(SGPE_ERR_ARG, why);
+    if (b->q_grid == 0) b->q_grid = sgpe::queue_resident_blocks();
+    if (b->q_grid <= 0) return fail(SGPE_ERR_CUDA, "work queue: no resident blocks on this device");
+    if (b->q_words == nullptr) {
+      const size_t words = 3 + b->plans.size() * 6 * kGraphSteps;
+      cudaError_t e = cudaMalloc(&b->q_words, sizeof(unsigned) * words);
+      if (e == cudaSuccess) e = cudaMemset(b->q_words, 0, sizeof(unsigned) * words);
+      if (e != cudaSuccess) return cuda_fail(e, "work queue counters");
+    }
+  }
+  if (bool(on) != b->queue) {
+    for (auto& x : b->graph)
+      if (x != nullptr) {
+        cudaGraphExecDestroy(x);
+        x = nullptr;
+      }
+    b->queue = bool(on);
+    b->q_direct = false;
+  }
+  return SGPE_OK;
+}
+
+int sgpe_batch_device_status(sgpe_batch* b, int* status) {
+  if (b == nullptr || status == nullptr) return fail(SGPE_ERR_ARG, "null batch or status");
+  *status = 0;
+  if (b->q_words == nullptr) return SGPE_OK;
+  DeviceGuard g(b->device);
+  int w = 0;
+  const cudaError_t e = cudaMemcpy(&w, b->q_words, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "batch status read");
+  *status = w;
+  if (w != 0) return fail(SGPE_ERR_CUDA, "a work-queue wait gave up (the batch's states are not reliable)");
+  return SGPE_OK;
+}
+
+int sgpe_check_queue_wait(int* gave_up, double* waited_ms) {
+  if (gave_up == nullptr || waited_ms == nullptr) return fail(SGPE_ERR_ARG, "null output");
+  const cudaError_t e = sgpe::check_queue_wait(gave_up, waited_ms);
+  return e == cudaSuccess ? SGPE_OK : cuda_fail(e, "queue wait check");
 }
 
 int sgpe_fft2(sgpe_plan* p, const void* i0, const void* i1, void* o0, void* o1, int inverse, double scale,

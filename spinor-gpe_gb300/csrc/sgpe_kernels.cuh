@@ -773,12 +773,23 @@ __device__ __forceinline__ TcScratch tc_setup(unsigned char* smem_raw, size_t ex
   return t;
 }
 
+// Position of a pass block among the blocks of its pass: block indices x
+// (lines or tiles) and y (the column pass's component), and the number of
+// x positions.  The pass kernels take it from the grid; the batch queue
+// kernel gives each work item its own.
+struct BlockPos {
+  int x, y, nx;
+};
+__device__ __forceinline__ BlockPos grid_pos() { return BlockPos{int(blockIdx.x), int(blockIdx.y), int(gridDim.x)}; }
+
 // SEP selects the point-wise code at compile time (separable operator
 // tables, RealOp::sep, or the generic broadcast fields), so each kernel
 // carries one of the two loops and stays small in the instruction cache.
 // TC: radix-16 stages on the tensor cores (complex64 only).
-template <typename R, int N, int E, int ROWS, bool SEP, bool TC = false>
-__device__ __forceinline__ void row_body(const RowArgs<R>& a) {
+// QUEUE: called by the batch queue kernel (plain loads and stores instead of
+// bulk copies: the state is written by other blocks of the same launch).
+template <typename R, int N, int E, int ROWS, bool SEP, bool TC = false, bool QUEUE = false>
+__device__ __forceinline__ void row_body(const RowArgs<R>& a, const BlockPos pos) {
   using C = Cx<R>;
   static_assert(!TC || sizeof(R) == 4, "tensor-core DFT16 is complex64 only");
   constexpr int T = N / E;
@@ -794,12 +805,12 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
   const int rho = tid / (2 * T);
   const int comp = (tid / T) & 1;
   const int j = tid % T;
-  const int y = blockIdx.x * ROWS + rho;
+  const int y = pos.x * ROWS + rho;
   const long long row_off = (long long)y * N;
 
   C v[1][E];
   const C* __restrict__ in = a.in[comp];
-  constexpr int kTma = N >= SGPE_ROW_TMA_MIN_N ? SGPE_ROW_TMA : 0;
+  constexpr int kTma = (N >= SGPE_ROW_TMA_MIN_N && !QUEUE) ? SGPE_ROW_TMA : 0;
   bool staged = false;
   if constexpr (kTma >= 1) {
     // The block's 2*ROWS input lines are staged by bulk copies into the
@@ -821,7 +832,7 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
         for (int c = 0; c < 2; ++c)
 #pragma unroll
           for (int r = 0; r < ROWS; ++r)
-            bulk_load(sm + (c * ROWS + r) * N, a.in[c] + (long long)(blockIdx.x * ROWS + r) * N, kLine, &s_bar);
+            bulk_load(sm + (c * ROWS + r) * N, a.in[c] + (long long)(pos.x * ROWS + r) * N, kLine, &s_bar);
       }
       staged = mbar_wait_bounded(&s_bar, 0);
       if (staged) {
@@ -857,7 +868,7 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
     // warps are not held up
     if (tid < 32) {
       double su0 = 0.0, su1 = 0.0;
-      const bool want_u = (a.pops != nullptr && blockIdx.x == 0);
+      const bool want_u = (a.pops != nullptr && pos.x == 0);
       const R l = a.fin != nullptr ? row_lambda_final(a.fin, R(a.norm_num), &su0, &su1)
                                    : row_lambda(a.part, a.ntile, tid, R(a.norm_num), &su0, &su1, want_u);
       if (tid == 0) {
@@ -945,7 +956,7 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
       for (int c = 0; c < 2; ++c)
 #pragma unroll
         for (int r = 0; r < ROWS; ++r)
-          bulk_store(a.out[c] + (long long)(blockIdx.x * ROWS + r) * N, sm + (c * ROWS + r) * N, kLine);
+          bulk_store(a.out[c] + (long long)(pos.x * ROWS + r) * N, sm + (c * ROWS + r) * N, kLine);
       bulk_commit();
       bulk_wait_read();
     }
@@ -959,7 +970,7 @@ __device__ __forceinline__ void row_body(const RowArgs<R>& a) {
 template <typename R, int N, int E, int ROWS, int MINB, bool SEP, bool TC = false>
 __global__ void __launch_bounds__(2 * (N / E) * ROWS, MINB)
 row_kernel(const RowArgs<R> a) {
-  row_body<R, N, E, ROWS, SEP, TC>(a);
+  row_body<R, N, E, ROWS, SEP, TC>(a, grid_pos());
 }
 
 // Several solves of one size in one launch (a batch): blockIdx.y selects the
@@ -967,12 +978,12 @@ row_kernel(const RowArgs<R> a) {
 template <typename R, int N, int E, int ROWS, int MINB, bool SEP>
 __global__ void __launch_bounds__(2 * (N / E) * ROWS, MINB)
 row_kernel_grouped(const RowArgs<R>* __restrict__ args) {
-  row_body<R, N, E, ROWS, SEP>(args[blockIdx.y]);
+  row_body<R, N, E, ROWS, SEP>(args[blockIdx.y], grid_pos());
 }
 
 // -------------------------------------------------------------- column pass
-template <typename R, int N, int E, int COLS, bool TC = false>
-__device__ __forceinline__ void col_body(const ColArgs<R>& a) {
+template <typename R, int N, int E, int COLS, bool TC = false, bool QUEUE = false>
+__device__ __forceinline__ void col_body(const ColArgs<R>& a, const BlockPos pos) {
   using C = Cx<R>;
   static_assert(!TC || sizeof(R) == 4, "tensor-core DFT16 is complex64 only");
   constexpr int T = N / E;
@@ -988,9 +999,9 @@ __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
   if constexpr (TC) __syncthreads();
   const int c = tid % COLS;
   const int j = tid / COLS;
-  const int comp = blockIdx.y;
+  const int comp = pos.y;
   const int nx = a.nx;
-  const int x = blockIdx.x * COLS + c;
+  const int x = pos.x * COLS + c;
   const int half = nx / 2;
   const int xin = a.in_shift ? (x + half) % nx : x;
   const int xout = a.out_shift ? (x + half) % nx : x;
@@ -1000,7 +1011,7 @@ __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
   C v[1][E];
   // TMA staging of the block's tile: rows of COLS complex values, row-major,
   // at a 128-byte aligned start of the exchange area
-  constexpr bool kTma = SGPE_COL_TMA && N >= SGPE_COL_TMA_MIN_N;
+  constexpr bool kTma = SGPE_COL_TMA && N >= SGPE_COL_TMA_MIN_N && !QUEUE;
   constexpr int kBoxY = N < 256 ? N : 256;
   constexpr uint32_t kTileBytes = uint32_t(COLS) * N * sizeof(C);
   static_assert(!kTma || sizeof(C) * COLS * (N / E + 2) >= 128, "the aligned tile must fit the exchange area");
@@ -1024,7 +1035,7 @@ __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
         mbar_arrive_expect_tx(&s_bar, kTileBytes);
 #pragma unroll
         for (int b = 0; b < N / kBoxY; ++b)
-          tensor_load_2d(stage + b * kBoxY * COLS, tmap, blockIdx.x * COLS * 2, b * kBoxY, &s_bar);
+          tensor_load_2d(stage + b * kBoxY * COLS, tmap, pos.x * COLS * 2, b * kBoxY, &s_bar);
       }
       staged = mbar_wait_bounded(&s_bar, 0);
       if (staged) {
@@ -1072,7 +1083,7 @@ __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
     if (tid == 0) {
 #pragma unroll
       for (int b = 0; b < N / kBoxY; ++b)
-        tensor_store_2d(tmap, blockIdx.x * COLS * 2, b * kBoxY, stage + b * kBoxY * COLS);
+        tensor_store_2d(tmap, pos.x * COLS * 2, b * kBoxY, stage + b * kBoxY * COLS);
       bulk_commit();
       bulk_wait_read();
     }
@@ -1098,7 +1109,7 @@ __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
       bu = warp_sum(bu);
       bw = warp_sum(bw);
       if (lane == 0) {
-        R* dst = a.part + 2 * ((long long)comp * gridDim.x + blockIdx.x);
+        R* dst = a.part + 2 * ((long long)comp * pos.nx + pos.x);
         dst[0] = bu;
         dst[1] = bw;
       }
@@ -1109,12 +1120,12 @@ __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
       if (tid == 0) {
         __threadfence();  // this block's partial is visible before its arrival
         const unsigned ticket = atomicAdd(a.count, 1u);
-        s_last = (ticket == gridDim.x * gridDim.y - 1);
+        s_last = (ticket == 2u * unsigned(pos.nx) - 1u);
       }
       __syncthreads();
       if (s_last) {
         __threadfence();
-        final_sums(static_cast<const R*>(a.part), int(gridDim.x), tid, NT, a.fin);
+        final_sums(static_cast<const R*>(a.part), pos.nx, tid, NT, a.fin);
         if (tid == 0) *a.count = 0u;
       }
     }
@@ -1124,14 +1135,14 @@ __device__ __forceinline__ void col_body(const ColArgs<R>& a) {
 template <typename R, int N, int E, int COLS, int MINB, bool TC = false>
 __global__ void __launch_bounds__((N / E) * COLS, MINB)
 col_kernel(const ColArgs<R> a) {
-  col_body<R, N, E, COLS, TC>(a);
+  col_body<R, N, E, COLS, TC>(a, grid_pos());
 }
 
 // Several solves of one size in one launch: blockIdx.z selects the solve.
 template <typename R, int N, int E, int COLS, int MINB>
 __global__ void __launch_bounds__((N / E) * COLS, MINB)
 col_kernel_grouped(const ColArgs<R>* __restrict__ args) {
-  col_body<R, N, E, COLS>(args[blockIdx.z]);
+  col_body<R, N, E, COLS>(args[blockIdx.z], grid_pos());
 }
 
 // Final k-space renormalisation of a materialised psik

@@ -17,7 +17,11 @@ from .pspinor import _native
 class PropagatorBatch:
     """A batch of ``TensorPropagator`` objects advanced together."""
 
-    def __init__(self, propagators):
+    def __init__(self, propagators, queue=False):
+        """``queue=True``: step the solves with one persistent launch fed
+        from a device work queue (``sgpe_batch_set_queue``; complex64 solves
+        with separable operators, sides 128-1024) instead of grouped
+        launches in parallel graph branches."""
         self.propagators = list(propagators)
         if not self.propagators:
             raise ValueError('a batch needs at least one propagator')
@@ -26,6 +30,13 @@ class PropagatorBatch:
             raise ValueError('all propagators of a batch must be on one device')
         self._device = devs.pop()
         self._batch = _native.Batch([p._plan for p in self.propagators])
+        self.queue = bool(queue)
+        if self.queue:
+            self._batch.set_queue(True)
+
+    def check_device(self):
+        """Raise ``SgpeError`` if a work-queue wait gave up (synchronous)."""
+        self._batch.check_device_status()
 
     def full_steps(self, n_steps):
         """Advance every solve by ``n_steps`` full Strang steps."""

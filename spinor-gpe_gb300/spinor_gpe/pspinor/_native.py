@@ -30,7 +30,8 @@ EXPORTED = ('sgpe_version', 'sgpe_last_error', 'sgpe_plan_create',
             'sgpe_set_dft_mode', 'sgpe_analysis', 'sgpe_setup_spinor',
             'sgpe_imprint_vortices', 'sgpe_fourier_split_x',
             'sgpe_shape_count', 'sgpe_set_shapes', 'sgpe_get_shapes',
-            'sgpe_autotune', 'sgpe_device_status', 'sgpe_check_bounded_wait')
+            'sgpe_autotune', 'sgpe_device_status', 'sgpe_check_bounded_wait',
+            'sgpe_batch_set_queue', 'sgpe_batch_device_status', 'sgpe_check_queue_wait')
 
 SGPE_MAX_SHAPES = 3
 # dtype_bits of the double-float precision (include/spinor_gb300.h)
@@ -92,6 +93,10 @@ _SIGS = {
                           ctypes.c_int),
     'sgpe_batch_destroy': ([_VP], ctypes.c_int),
     'sgpe_batch_steps': ([_VP, ctypes.c_int, _VP], ctypes.c_int),
+    'sgpe_batch_set_queue': ([_VP, ctypes.c_int], ctypes.c_int),
+    'sgpe_batch_device_status': ([_VP, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+    'sgpe_check_queue_wait': ([ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)],
+                              ctypes.c_int),
     'sgpe_set_dft_mode': ([_VP, ctypes.c_int], ctypes.c_int),
     'sgpe_shape_count': ([ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     'sgpe_device_status': ([_VP, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
@@ -354,3 +359,13 @@ class Batch:
     def steps(self, torch, n_steps, device):
         check(load().sgpe_batch_steps(self._h, int(n_steps),
                                       _stream(torch, device)))
+
+    def set_queue(self, on):
+        """Work-queue mode: the steps run as one persistent launch of the
+        queue kernel per graph (complex64 plans with separable operators)."""
+        check(load().sgpe_batch_set_queue(self._h, int(bool(on))))
+
+    def check_device_status(self):
+        """Raise if a work-queue wait gave up (synchronous)."""
+        st = ctypes.c_int()
+        check(load().sgpe_batch_device_status(self._h, ctypes.byref(st)))

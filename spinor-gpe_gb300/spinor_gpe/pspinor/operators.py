@@ -196,6 +196,24 @@ class Decomposition:
         else:
             self.kind, self.vals = 'full', e
 
+    @classmethod
+    def with_y_table(cls, energy, b, ulps=8):
+        """The separable decomposition of ``energy`` with the given y-table
+        ``b`` (a(x) = energy[0, :] - b[0]), or None when energy[y, x]
+        differs from a[x] + b[y] by more than ``ulps`` FP64 ulps of
+        max|energy| (the tolerance of ``split_separable``)."""
+        e = np.asarray(energy, dtype=np.float64)
+        b = np.asarray(b, dtype=np.float64)
+        a = e[0, :] - b[0]
+        resid = np.abs(e - (a[None, :] + b[:, None]))
+        scale = max(float(np.max(np.abs(e))), np.finfo(np.float64).tiny)
+        if np.max(resid) > ulps * np.finfo(np.float64).eps * scale:
+            return None
+        d = cls.__new__(cls)
+        d.shape = e.shape
+        d.kind, d.vals = 'sep', (a, b)
+        return d
+
 
 def _decomposed(energy):
     return energy if isinstance(energy, Decomposition) else Decomposition(energy)
@@ -319,7 +337,17 @@ class Prepared:
             same = False
         else:
             same = np.array_equal(f[1], f[0])
-        return [d0, d0] if same else [d0, Decomposition(f[1])]
+        if same:
+            return [d0, d0]
+        d1 = Decomposition(f[1])
+        if d0.kind == 'sep' and d1.kind == 'sep' and not isinstance(f[1], SepField):
+            # fields that differ by a constant (a uniform detuning) share
+            # the first one's y-table, so that the two components' y
+            # factors are proportional exactly and not only to rounding of
+            # the independent splits (large trap energies at the grid edge
+            # leave the independent tables ulps apart)
+            d1 = Decomposition.with_y_table(f[1], d0.vals[1]) or d1
+        return [d0, d1]
 
 
 def build_substep(t_sub, kin_eng_spin, pot_eng_spin, coupling, expon, outer,

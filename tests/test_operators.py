@@ -82,3 +82,28 @@ def test_coupling_energy_spec_matches_dense():
     np.testing.assert_allclose(spec.dense(NY, NX), omega / 2 * np.exp(-1.0j * theta), rtol=0, atol=1e-15)
     spec = ops.coupling_energy_spec(omega, None, NX)
     assert spec.kind == 'uniform'
+
+
+def test_detuned_components_share_the_y_table():
+    """Potentials that differ by a uniform detuning (V + delta/2, V - delta/2)
+    share one y-table even where a large trap energy at the grid edge leaves
+    independent splits ulps apart, so their y factors are exactly
+    proportional; each split still reproduces its field to 8 ulps."""
+    x = np.arange(-64.0, 64.0, 0.125)
+    X, Y = np.meshgrid(x, x)
+    V = 0.5 * (X ** 2 + (1.909 * Y) ** 2)
+    pot = [V + 0.43 / 2, V - 0.43 / 2]
+    d0, d1 = ops.Prepared([np.zeros_like(V)] * 2, pot, np.zeros_like(V), None).pot
+    assert d0.kind == d1.kind == 'sep'
+    assert d1.vals[1] is d0.vals[1]
+    for d, e in zip((d0, d1), pot):
+        a, b = d.vals
+        resid = np.abs(e - (a[None, :] + b[:, None]))
+        assert resid.max() <= 8 * np.finfo(np.float64).eps * np.abs(e).max()
+    p0 = ops.phase_op(d0, 0.008)[1].values
+    p1 = ops.phase_op(d1, 0.008)[1].values
+    np.testing.assert_array_equal(p0, p1)
+    # a field that is not the first plus a constant keeps its own split
+    other = 0.5 * (X ** 2 + (1.5 * Y) ** 2)
+    e0, e1 = ops.Prepared([np.zeros_like(V)] * 2, [V, other], np.zeros_like(V), None).pot
+    assert e1.vals[1] is not e0.vals[1]

@@ -51,6 +51,13 @@ def test_argument_errors_without_gpu(native_lib):
     assert lib.sgpe_set_dft_mode(None, 1) == _native.SGPE_ERR_ARG
     with pytest.raises(_native.SgpeError):
         _native.check(lib.sgpe_single_step(None, 0, None))
+    # batch and work-queue entry points
+    st = ctypes.c_int(-1)
+    assert lib.sgpe_batch_steps(None, 1, None) == _native.SGPE_ERR_ARG
+    assert lib.sgpe_batch_set_queue(None, 1) == _native.SGPE_ERR_ARG
+    assert lib.sgpe_batch_device_status(None, ctypes.byref(st)) == _native.SGPE_ERR_ARG
+    assert lib.sgpe_check_queue_wait(None, None) == _native.SGPE_ERR_ARG
+    assert lib.sgpe_batch_destroy(None) == _native.SGPE_OK
     assert lib.sgpe_version() >= 100
 
 

@@ -76,21 +76,23 @@ template <> struct Tune<double> {
   static constexpr int COL_MAX_THREADS = 1024, COL_MINB_LARGE = 1;
 };
 // Double-float: a complex value is four FP32 registers, so 8 points per
-// thread (12 for sides 3 * 2^k); three 256-thread row blocks per SM (80
-// registers) and 2-column tiles with three blocks per SM, measured on GB300
-// at 1024^2 against two row blocks and 4-column tiles with one (row pass
-// 107 -> 99 us, column pass 75 -> 68 us).
+// thread (12 for sides 3 * 2^k); 256-thread row blocks and 2-column tiles,
+// four blocks per SM (64 registers at 1024; no row spills, 16 bytes of
+// column spills).  Measured on GB300 at 1024^2: two row blocks and 4-column
+// tiles with one block -> three of each: row pass 107 -> 99 us, column pass
+// 75 -> 68 us; three -> four of each (later build): column pass 75.7 ->
+// 73.0 us, row pass 85.3 -> 85.0 us, 2,183 -> 2,240 steps/s.
 #ifndef SGPE_DF_ROW_THREADS
 #define SGPE_DF_ROW_THREADS 256
 #endif
 #ifndef SGPE_DF_ROW_MINB
-#define SGPE_DF_ROW_MINB 3
+#define SGPE_DF_ROW_MINB 4
 #endif
 #ifndef SGPE_DF_COLS
 #define SGPE_DF_COLS 2
 #endif
 #ifndef SGPE_DF_COL_MINB
-#define SGPE_DF_COL_MINB 3
+#define SGPE_DF_COL_MINB 4
 #endif
 // Sides of 2048 and more: one 512-thread block per SM for rows and at most
 // 512-thread column blocks, so that the 128-register cap holds (no spills).

@@ -67,10 +67,21 @@ template <> struct Tune<float> {
   static constexpr int R3_E_LARGE = SGPE_F32_R3_E_LARGE, R3_COL_MINB_LARGE = SGPE_F32_R3_COL_MINB_LARGE;
   static constexpr int COL_MAX_THREADS = 1024, COL_MINB_LARGE = SGPE_F32_COL_MINB;
 };
+// complex128: two 256-thread row blocks (128 registers; at three the
+// generic-operator row kernels spill) and two 512-thread column blocks (64
+// registers) per SM; measured on GB300 at 1024^2, two column blocks against
+// one: column pass 351.7 -> 346.7 us (the passes are bound by the FP64
+// pipe; 256^2 unchanged).
+#ifndef SGPE_F64_ROW_MINB
+#define SGPE_F64_ROW_MINB 2
+#endif
+#ifndef SGPE_F64_COL_MINB
+#define SGPE_F64_COL_MINB 2
+#endif
 template <> struct Tune<double> {
-  static constexpr int ROW_E = 8, ROW_THREADS = 256, ROW_MINB = 2;
+  static constexpr int ROW_E = 8, ROW_THREADS = 256, ROW_MINB = SGPE_F64_ROW_MINB;
   static constexpr int ROW_E_LARGE = 8, ROW_MINB_LARGE = 2;
-  static constexpr int COL_E = 8, COLS = 4, COL_MINB = 1;
+  static constexpr int COL_E = 8, COLS = 4, COL_MINB = SGPE_F64_COL_MINB;
   static constexpr int R3_E = 12, R3_ROW_MINB = 2, R3_COL_MINB = 1;
   static constexpr int R3_E_LARGE = 12, R3_COL_MINB_LARGE = 1;
   static constexpr int COL_MAX_THREADS = 1024, COL_MINB_LARGE = 1;

@@ -276,6 +276,15 @@ inline cudaError_t launch_pdl(K kernel, dim3 grid, dim3 block, size_t smem, cuda
 #endif
 }
 
+// Resident row blocks per SM requested for a kernel: the configuration's,
+// except for the double-float rows with generic operator fields, whose
+// point-wise code needs more registers (at the separable kernels' 64 they
+// spill 200+ bytes): three blocks below 2048, one from 2048.
+template <typename R, bool SEP, int N> constexpr int row_minb(int cfg_minb) {
+  if constexpr (is_df<R>::value && !SEP) return cmin(cfg_minb, N >= 2048 ? 1 : 3);
+  return cfg_minb;
+}
+
 template <typename R, bool SEP, int S> struct RowLauncher {
   const RowArgs<R>* a;
   int ny;
@@ -286,7 +295,7 @@ template <typename R, bool SEP, int S> struct RowLauncher {
       return cudaErrorInvalidValue;
     } else {
       if (ny % Cfg::ROWS != 0) return cudaErrorInvalidValue;
-      auto k = row_kernel<R, N, Cfg::E, Cfg::ROWS, Cfg::MINB, SEP>;
+      auto k = row_kernel<R, N, Cfg::E, Cfg::ROWS, row_minb<R, SEP, N>(Cfg::MINB), SEP>;
       static unsigned long long done = 0;
       cudaError_t e = smem_limit_once(k, Cfg::SMEM, &done);
       if (e != cudaSuccess) return e;

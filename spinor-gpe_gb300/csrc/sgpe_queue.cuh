@@ -21,9 +21,10 @@
 // col_body), with the item's position instead of the block's, plain loads
 // and stores of the state (no bulk copies: the state was written by other
 // blocks of this launch), in fixed 512-thread shapes per line length.
-// Producers publish a finished item as the grid-synchronisation pattern
-// does (block barrier, then one thread's device-scope fence and arrival);
-// consumers read the counter with acquire loads, fence, then barrier, after
+// Blocks claim SGPE_QUEUE_CHUNK consecutive items at a time.  Producers
+// publish finished items with a block barrier followed by one thread's
+// device-scope release reduction on the phase's counter; consumers read the
+// counter with device-scope acquire loads, then pass a block barrier, after
 // which the block's plain loads see the producers' stores.
 #pragma once
 #include "sgpe_kernels.cuh"
